@@ -1,0 +1,160 @@
+// Test infrastructure: drives the unmodified reference library (trenki2/SoftwareRenderer
+// src/renderer, compiled from its own sources by oracle/Makefile) through the same
+// oracle_draw() entry point as the CPU port, using the shared shader programs of
+// swr_programs.h wrapped in the reference's VertexShaderBase / PixelShaderBase.
+// Used to generate the golden fixtures under tests/golden and to pin the port.
+#include <stdint.h>
+#include <string.h>
+#include <vector>
+#include "Renderer.h"  // reference umbrella header (src/renderer/Renderer.h)
+#include "oracle_abi.h"
+
+namespace {
+
+const SwrUniforms* g_u = nullptr;  // the reference keeps shader parameters in statics
+int g_prim = 0;
+uint64_t g_frags = 0, g_outside = 0;
+
+template <class P>
+struct RefPS : public swr::PixelShaderBase<RefPS<P>> {
+  static const int AVarCount = P::AVarCount;
+  static const int PVarCount = P::PVarCount;
+  static const int InterpolateZ = P::InterpolateZ;
+  static const int InterpolateW = P::InterpolateW;
+  static void drawPixel(const swr::PixelData& p) {
+    if (p.x < 0 || p.y < 0 || p.x >= g_u->width || p.y >= g_u->height) {
+      g_outside++;
+      return;
+    }
+    typename P::State s;
+    P::load(s, p.x, p.y, *g_u);
+    P::drawPixel(p, g_prim, s, *g_u);
+    P::store(s, p.x, p.y, *g_u);
+    g_frags++;
+  }
+};
+
+template <class V>
+struct RefVS : public swr::VertexShaderBase<RefVS<V>> {
+  static const int AttribCount = V::AttribCount;
+  static const int AVarCount = V::AVarCount;
+  static const int PVarCount = V::PVarCount;
+  static void processVertex(swr::VertexShaderInput in, swr::VertexShaderOutput* out) {
+    SwrVertexInput vi;
+    for (int i = 0; i < V::AttribCount; ++i) vi.p[i] = in[i];
+    V::processVertex(vi, out, *g_u);
+  }
+};
+
+// IRasterizer that numbers the primitives it forwards (the same loops as
+// Rasterizer::draw*List) so the pixel shader can record which primitive wrote a pixel.
+class NumberingRasterizer : public swr::IRasterizer {
+ public:
+  explicit NumberingRasterizer(swr::Rasterizer* r) : r_(r) {}
+  mutable uint64_t prims = 0;
+  void drawPointList(const swr::RasterizerVertex* v, const int* idx, size_t n) const override {
+    for (size_t i = 0; i < n; ++i) {
+      if (idx[i] == -1) continue;
+      g_prim = (int)prims++;
+      r_->drawPoint(v[idx[i]]);
+    }
+  }
+  void drawLineList(const swr::RasterizerVertex* v, const int* idx, size_t n) const override {
+    for (size_t i = 0; i + 2 <= n; i += 2) {
+      if (idx[i] == -1) continue;
+      g_prim = (int)prims++;
+      r_->drawLine(v[idx[i]], v[idx[i + 1]]);
+    }
+  }
+  void drawTriangleList(const swr::RasterizerVertex* v, const int* idx, size_t n) const override {
+    for (size_t i = 0; i + 3 <= n; i += 3) {
+      if (idx[i] == -1) continue;
+      g_prim = (int)prims++;
+      r_->drawTriangle(v[idx[i]], v[idx[i + 1]], v[idx[i + 2]]);
+    }
+  }
+
+ private:
+  swr::Rasterizer* r_;
+};
+
+template <class V>
+void set_vs(swr::VertexProcessor& vp) {
+  vp.setVertexShader<RefVS<V>>();
+}
+
+template <class P>
+void set_ps(swr::Rasterizer& r) {
+  r.setPixelShader<RefPS<P>>();
+}
+
+}  // namespace
+
+extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
+  if (!d || !d->uniforms) return 1;
+  const uint64_t per = d->draw_mode == 0 ? 1 : (d->draw_mode == 1 ? 2 : 3);
+  if (d->draw_mode < 0 || d->draw_mode > 2 || d->count % per) return 1;
+  for (uint64_t i = 0; i < d->count; ++i)
+    if (d->indices[i] < (d->raster_vertices ? -1 : 0)) return 1;
+  g_u = d->uniforms;
+  g_frags = g_outside = 0;
+  g_prim = 0;
+
+  swr::Rasterizer r;
+  r.setRasterMode(d->raster_mode == 0 ? swr::RasterMode::Span
+                  : d->raster_mode == 1 ? swr::RasterMode::Block
+                                        : swr::RasterMode::Adaptive);
+  r.setScissorRect(d->scissor[0], d->scissor[1], d->scissor[2], d->scissor[3]);
+  switch (d->ps_id) {
+    case SWR_PS_TEX_NEAREST: set_ps<PsTexNearest>(r); break;
+    case SWR_PS_LAMBERT: set_ps<PsLambert>(r); break;
+    case SWR_PS_VCOLOR: set_ps<PsVColor>(r); break;
+    case SWR_PS_VCOLOR_AFFINE: set_ps<PsVColorAffine>(r); break;
+    case SWR_PS_LAMBERT_TEX: set_ps<PsLambertTex>(r); break;
+    case SWR_PS_DIFF: set_ps<PsDiff>(r); break;
+    default: return 2;
+  }
+  NumberingRasterizer nr(&r);
+  // The reference flushes a batch every 1024 primitives plus once at the end
+  // (VertexProcessor.cpp:110-119); counted here for comparison with the port.
+  const uint64_t batches = d->raster_vertices ? 0 : d->count / per / 1024 + 1;
+  if (d->raster_vertices) {
+    int maxi = -1;
+    for (uint64_t i = 0; i < d->count; ++i) maxi = d->indices[i] > maxi ? d->indices[i] : maxi;
+    std::vector<swr::RasterizerVertex> v((size_t)(maxi + 1));
+    if (maxi >= 0) memcpy(v.data(), d->raster_vertices, v.size() * sizeof(swr::RasterizerVertex));
+    if (d->draw_mode == 0) nr.drawPointList(v.data(), d->indices, d->count);
+    else if (d->draw_mode == 1) nr.drawLineList(v.data(), d->indices, d->count);
+    else nr.drawTriangleList(v.data(), d->indices, d->count);
+  } else {
+    swr::VertexProcessor vp(&nr);
+    vp.setViewport(d->viewport[0], d->viewport[1], d->viewport[2], d->viewport[3]);
+    vp.setDepthRange(d->depth_range[0], d->depth_range[1]);
+    vp.setCullMode(d->cull_mode == 0 ? swr::CullMode::None
+                   : d->cull_mode == 1 ? swr::CullMode::CCW
+                                       : swr::CullMode::CW);
+    switch (d->vs_id) {
+      case SWR_VS_POS_UV: set_vs<VsPosUV>(vp); break;
+      case SWR_VS_POS_NRM_UV: set_vs<VsPosNrmUV>(vp); break;
+      case SWR_VS_POS_RGB: set_vs<VsPosRGB>(vp); break;
+      case SWR_VS_POS_RGB_AFFINE: set_vs<VsPosRGBAffine>(vp); break;
+      case SWR_VS_POS_RGB_UV: set_vs<VsPosRGBUV>(vp); break;
+      default: return 2;
+    }
+    for (int a = 0; a < 8; ++a)
+      if (d->attrib[a]) vp.setVertexAttribPointer(a, d->attrib_stride[a], d->attrib[a]);
+    vp.drawElements(swr::DrawMode(d->draw_mode == 0 ? swr::DrawMode::Point
+                                  : d->draw_mode == 1 ? swr::DrawMode::Line
+                                                      : swr::DrawMode::Triangle),
+                    (size_t)d->count, const_cast<int*>(d->indices));
+  }
+  if (st) {
+    st->fragments = g_frags;
+    st->outside = g_outside;
+    st->primitives = nr.prims;
+    st->batches = batches;
+  }
+  return 0;
+}
+
+extern "C" float oracle_fold(float v, float a, int k) { return swr_fold(v, a, k); }
