@@ -1,0 +1,106 @@
+/* swr_gb300 — C ABI of the GB300 rasterization pipeline.
+ *
+ * A drop-in for the VertexProcessor + Rasterizer path of trenki2/SoftwareRenderer
+ * (src/renderer/).  One swr_context holds the state that a VertexProcessor and a
+ * Rasterizer hold together; every entry point names the reference member it replaces.
+ * Shaders are compiled into the library as built-in programs (the reference binds them
+ * as template arguments, setVertexShader<VS> / setPixelShader<PS>); their uniforms,
+ * including the render target buffers that the reference's pixel shaders keep in
+ * statics, travel in SwrUniforms (softwarerenderer_gb300/csrc/swr_programs.h).
+ *
+ * Memory: every buffer pointer passed here (attributes, indices, RasterizerVertex arrays,
+ * the colour/depth/texture pointers inside SwrUniforms) is a CUDA device pointer.  The
+ * context owns its scratch (post-transform vertices, clip table, bins) and grows it on
+ * demand.  Draws are queued asynchronously on the given stream (NULL = legacy default
+ * stream); swr_finish() waits and reports.  Errors are returned, never asserted.
+ * A context is not reentrant (like VertexProcessor, VertexProcessor.h:146-151): use one
+ * context per host thread / stream.
+ */
+#ifndef SWR_GB300_H
+#define SWR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define SWR_OK 0
+#define SWR_EINVAL 1     /* invalid argument (the reference asserts or has undefined behaviour) */
+#define SWR_ENOMEM 2     /* device allocation failed */
+#define SWR_EOVERFLOW 3  /* a scratch queue was too small: the draw left its targets untouched,
+                            the context has grown the queue; issue the draw again */
+#define SWR_ECUDA 4      /* CUDA runtime error */
+#define SWR_EINDEX 5     /* an index addressed a vertex beyond the bound attribute buffers */
+
+/* Enumerations carry the reference's values. */
+#define SWR_DRAW_POINT 0     /* DrawMode::Point    (VertexProcessor.h:42-46) */
+#define SWR_DRAW_LINE 1      /* DrawMode::Line */
+#define SWR_DRAW_TRIANGLE 2  /* DrawMode::Triangle */
+#define SWR_CULL_NONE 0      /* CullMode::None     (VertexProcessor.h:49-53) */
+#define SWR_CULL_CCW 1       /* CullMode::CCW */
+#define SWR_CULL_CW 2        /* CullMode::CW (the reference's default) */
+#define SWR_RASTER_SPAN 0    /* RasterMode::Span   (Rasterizer.h:45-49, default) */
+#define SWR_RASTER_BLOCK 1   /* RasterMode::Block */
+#define SWR_RASTER_ADAPTIVE 2 /* RasterMode::Adaptive */
+
+typedef struct swr_context swr_context;
+struct SwrUniforms; /* softwarerenderer_gb300/csrc/swr_programs.h */
+
+typedef struct swr_stats {
+  uint64_t fragments;   /* drawPixel calls since the last swr_finish */
+  uint64_t primitives;  /* primitives handed to the rasterizer by the last draw */
+  uint64_t bin_pairs;   /* (tile, primitive) bin entries of the last draw */
+  uint32_t clip_polygons;  /* triangles clipped against the frustum in the last draw */
+  uint32_t flags;       /* internal status bits (0 when everything succeeded) */
+} swr_stats;
+
+/* Context lifetime.  Replaces constructing VertexProcessor(IRasterizer*) + Rasterizer()
+ * (VertexProcessor.cpp:29-35, Rasterizer.h:67-72): defaults are CullMode::CW, depth range
+ * (0, 1), RasterMode::Span, scissor (0, 0, 0, 0), tile size 16. */
+int swr_create(swr_context** out);
+int swr_destroy(swr_context* ctx);
+
+/* VertexProcessor::setViewport (VertexProcessor.h:66, VertexProcessor.cpp:43-54). */
+int swr_set_viewport(swr_context* ctx, int x, int y, int width, int height);
+/* VertexProcessor::setDepthRange (VertexProcessor.h:70, VertexProcessor.cpp:56-60). */
+int swr_set_depth_range(swr_context* ctx, float n, float f);
+/* VertexProcessor::setCullMode (VertexProcessor.h:74, VertexProcessor.cpp:62-65). */
+int swr_set_cull_mode(swr_context* ctx, int mode);
+/* VertexProcessor::setVertexShader<VS> (VertexProcessor.h:77-85): built-in VS id. */
+int swr_set_vertex_shader(swr_context* ctx, int vs_id);
+/* VertexProcessor::setVertexAttribPointer (VertexProcessor.h:88, VertexProcessor.cpp:67-76).
+ * `bytes` is the buffer size; the vertex count used for index bounds checks is
+ * bytes / stride (the reference does not check indices). */
+int swr_set_vertex_attrib_pointer(swr_context* ctx, int index, int stride, const void* buffer,
+                                  uint64_t bytes);
+/* VertexProcessor::drawElements (VertexProcessor.h:91, VertexProcessor.cpp:78-120).
+ * indices: device uint32 array; values must be < 2^31 - 1 (the reference's int). */
+int swr_draw_elements(swr_context* ctx, int mode, uint64_t count, const uint32_t* indices,
+                      void* stream);
+
+/* Rasterizer::setRasterMode (Rasterizer.h:75-78). */
+int swr_set_raster_mode(swr_context* ctx, int mode);
+/* Rasterizer::setScissorRect (Rasterizer.h:81-87). */
+int swr_set_scissor_rect(swr_context* ctx, int x, int y, int width, int height);
+/* Rasterizer::setPixelShader<PS> (Rasterizer.h:90-96): built-in PS id. */
+int swr_set_pixel_shader(swr_context* ctx, int ps_id);
+/* Shader uniforms and render target (the reference's shader statics).  Copied. */
+int swr_set_uniforms(swr_context* ctx, const struct SwrUniforms* u);
+/* IRasterizer::draw{Point,Line,Triangle}List (IRasterizer.h:56-71, Rasterizer.h:116-141):
+ * vertices are RasterizerVertex records (x, y, z, w, avar[16], pvar[16]; 36 floats) in
+ * screen space; an index of -1 at the start of a primitive skips it. */
+int swr_draw_list(swr_context* ctx, int mode, const float* vertices, uint64_t nverts,
+                  const int32_t* indices, uint64_t count, void* stream);
+
+/* Wait for the stream, report and reset the accumulated status. */
+int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
+/* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels. */
+int swr_set_tile_size(swr_context* ctx, int tile);
+const char* swr_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWR_GB300_H */

@@ -1,0 +1,463 @@
+// C ABI and draw orchestration: the host side of VertexProcessor::drawElements and
+// Rasterizer::draw*List for the GPU pipeline.  One draw is a fixed sequence of kernels on
+// one stream whose variable sizes (clip output, primitives, bin pairs) stay on the
+// device; overflow of a scratch queue is detected on the device, skips the raster stage
+// and is reported by swr_finish, which grows the queue for the next attempt.
+#include <stdio.h>
+#include <string.h>
+#include <vector>
+#include "../../include/swr_gb300.h"
+#include "swr_core.h"
+#include "swr_ops.h"
+
+namespace swr {
+
+// Status buffer: words [0, SWR_ST_WORDS) as in swr_device.cuh; words 8..12 hold the
+// largest per-draw requests seen since the last finish.
+constexpr int kStatusWords = 16;
+constexpr int kStickyBase = 8;
+
+__global__ void k_close_draw(uint32_t* st) {
+  for (int i = SWR_ST_CLIP_SLOTS; i <= SWR_ST_FRAGS; ++i) {
+    const uint32_t v = st[i];
+    if (v > st[kStickyBase + i]) st[kStickyBase + i] = v;
+  }
+}
+
+struct Buffer {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~Buffer() {
+    if (p) cudaFree(p);
+  }
+  bool ensure(size_t n) {
+    if (n <= bytes) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = n + n / 4;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    bytes = want;
+    return true;
+  }
+  template <class T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+struct Attrib {
+  const void* ptr = nullptr;
+  int stride = 0;
+  uint64_t bytes = 0;
+};
+
+}  // namespace swr
+
+struct swr_context {
+  // VertexProcessor state
+  int vp_x = 0, vp_y = 0, vp_w = 0, vp_h = 0;
+  float dn = 0.0f, df = 1.0f;
+  int cull = SWR_CULL_CW;
+  int vs_id = 0;
+  swr::Attrib attribs[8];
+  // Rasterizer state
+  int raster_mode = SWR_RASTER_SPAN;
+  int sc_x = 0, sc_y = 0, sc_w = 0, sc_h = 0;
+  int ps_id = 0;
+  SwrUniforms u;
+  bool have_u = false;
+  int tile = 16;
+  // capacities of the device-sized queues
+  uint32_t cap_prims = 0, cap_clip_slots = 0, cap_clip_verts = 0, cap_pairs = 0;
+  // device buffers
+  swr::Buffer draws, targets, draw_vbase, draw_bbase, target_tile_base;
+  swr::Buffer ptv, clipv, clip_table, clip_slot, tri_flags, batch_counts, batch_base;
+  swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
+  swr::Buffer scratch, status, direct_keep, direct_pos;
+  uint32_t* status_host = nullptr;
+  uint32_t last_ntiles = 0;
+};
+
+namespace {
+
+using namespace swr;
+
+int cuda_err(cudaError_t e) {
+  if (e == cudaSuccess) return SWR_OK;
+  fprintf(stderr, "swr_gb300: CUDA error %s\n", cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? SWR_ENOMEM : SWR_ECUDA;
+}
+
+int bits_for(uint32_t n) {
+  int b = 0;
+  while (b < 32 && (1ull << b) < (uint64_t)n) ++b;
+  return b;
+}
+
+bool grow_u32(uint32_t& cap, uint64_t need) {
+  if (need <= cap) return true;
+  uint64_t c = need + need / 4 + 1024;
+  if (c > 0xffffffffull) return false;
+  cap = (uint32_t)c;
+  return true;
+}
+
+// Allocates every queue a draw with the given host-known sizes needs.
+int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, uint32_t nbatches,
+                    uint32_t ntiles, int R) {
+  grow_u32(c->cap_prims, (uint64_t)nsub + 1024);
+  grow_u32(c->cap_clip_slots, (uint64_t)nsub / 16 + 1024);
+  grow_u32(c->cap_clip_verts, (uint64_t)c->cap_clip_slots * 4);
+  grow_u32(c->cap_pairs, (uint64_t)c->cap_prims * 2 + 65536);
+  bool ok = true;
+  ok &= c->ptv.ensure((size_t)nverts_ptv * S * 4 + 16);
+  ok &= c->clipv.ensure((size_t)c->cap_clip_verts * S * 4 + 16);
+  ok &= c->clip_table.ensure((size_t)c->cap_clip_slots * sizeof(SwrClipEntry) + 16);
+  ok &= c->clip_slot.ensure((size_t)nsub * 4 + 16);
+  ok &= c->tri_flags.ensure((size_t)nsub + 16);
+  ok &= c->batch_counts.ensure((size_t)nbatches * 8 + 16);
+  ok &= c->batch_base.ensure((size_t)nbatches * 4 + 16);
+  ok &= c->tris.ensure((size_t)c->cap_prims * 16 + 16);
+  ok &= c->recs.ensure((size_t)c->cap_prims * R * 4 + 16);
+  ok &= c->tile_count.ensure((size_t)c->cap_prims * 4 + 16);
+  ok &= c->pair_off.ensure((size_t)c->cap_prims * 4 + 16);
+  ok &= c->keys0.ensure((size_t)c->cap_pairs * 4 + 16);
+  ok &= c->vals0.ensure((size_t)c->cap_pairs * 4 + 16);
+  ok &= c->keys1.ensure((size_t)c->cap_pairs * 4 + 16);
+  ok &= c->vals1.ensure((size_t)c->cap_pairs * 4 + 16);
+  ok &= c->tile_start.ensure((size_t)(ntiles + 1) * 4 + 16);
+  const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64;
+  ok &= c->scratch.ensure(sw * 4);
+  ok &= c->draws.ensure(sizeof(SwrDrawDesc));
+  ok &= c->targets.ensure(sizeof(SwrTargetDesc));
+  ok &= c->draw_vbase.ensure(64);
+  ok &= c->draw_bbase.ensure(64);
+  ok &= c->target_tile_base.ensure(64);
+  return ok ? SWR_OK : SWR_ENOMEM;
+}
+
+void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
+  memset(&D, 0, sizeof(D));
+  for (int a = 0; a < 8; ++a) {
+    D.attrib[a] = c->attribs[a].ptr;
+    D.attrib_stride[a] = c->attribs[a].stride;
+  }
+  D.draw_mode = mode;
+  D.cull = c->cull;
+  D.raster_mode = c->raster_mode;
+  D.vp_px = (float)c->vp_w / 2.0f;  // VertexProcessor::setViewport
+  D.vp_py = (float)c->vp_h / 2.0f;
+  D.vp_ox = (float)c->vp_x + D.vp_px;
+  D.vp_oy = (float)c->vp_y + D.vp_py;
+  D.dn = c->dn;
+  D.df = c->df;
+  D.sc_minx = c->sc_x;
+  D.sc_miny = c->sc_y;
+  D.sc_maxx = c->sc_x + c->sc_w;
+  D.sc_maxy = c->sc_y + c->sc_h;
+  D.u = c->u;
+}
+
+// Setup, binning and tile raster for the primitives in c->tris (count on the device).
+int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int vs_a, int vs_p,
+                 uint32_t ntiles, cudaStream_t s) {
+  uint32_t* st = c->status.as<uint32_t>();
+  SetupArgs sa;
+  sa.tris = c->tris.as<uint4>();
+  sa.status = st;
+  sa.cap_prims = c->cap_prims;
+  sa.ptv = c->ptv.as<float>();
+  sa.clipv = c->clipv.as<float>();
+  sa.S = S;
+  sa.off_a = off_a;
+  sa.off_p = off_p;
+  sa.vs_a = vs_a;
+  sa.vs_p = vs_p;
+  sa.draws = c->draws.as<SwrDrawDesc>();
+  sa.targets = c->targets.as<SwrTargetDesc>();
+  sa.recs = c->recs.as<float>();
+  sa.tile_count = c->tile_count.as<uint32_t>();
+  sa.tile = c->tile;
+  ps->setup(sa, s);
+  uint32_t* scr = c->scratch.as<uint32_t>();
+  uint32_t* sort_scr = scr + scan_scratch_words(c->cap_prims) + 32;
+  scan_exclusive(c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(), st + SWR_ST_PRIMS, c->cap_prims,
+                 st + SWR_ST_PAIRS, scr, s);
+  ps->emit_pairs(st, c->cap_prims, c->recs.as<float>(), c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(),
+                 st + SWR_ST_PAIRS, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
+                 c->tile, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), st, s);
+  const int which = radix_sort_pairs(c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), c->keys1.as<uint32_t>(),
+                                     c->vals1.as<uint32_t>(), st + SWR_ST_PAIRS, c->cap_pairs,
+                                     bits_for(ntiles), sort_scr, s);
+  uint32_t* keys = which ? c->keys1.as<uint32_t>() : c->keys0.as<uint32_t>();
+  uint32_t* vals = which ? c->vals1.as<uint32_t>() : c->vals0.as<uint32_t>();
+  segment_starts(keys, st + SWR_ST_PAIRS, c->cap_pairs, ntiles, c->tile_start.as<uint32_t>(), s);
+  RasterArgs ra;
+  ra.status = st;
+  ra.tile_start = c->tile_start.as<uint32_t>();
+  ra.bin = vals;
+  ra.recs = c->recs.as<float>();
+  ra.draws = c->draws.as<SwrDrawDesc>();
+  ra.targets = c->targets.as<SwrTargetDesc>();
+  ra.target_tile_base = c->target_tile_base.as<uint32_t>();
+  ra.ntargets = 1;
+  ra.status_w = st;
+  ps->raster(ra, ntiles, c->tile, s);
+  k_close_draw<<<1, 1, 0, s>>>(st);
+  return cuda_err(cudaGetLastError());
+}
+
+int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, cudaStream_t s) {
+  const uint32_t zero = 0;
+  cudaMemcpyAsync(c->draws.p, &D, sizeof(D), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(c->targets.p, &T, sizeof(T), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(c->draw_vbase.p, &zero, 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(c->draw_bbase.p, &zero, 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(c->target_tile_base.p, &zero, 4, cudaMemcpyHostToDevice, s);
+  // reset the per-draw working counters (flags and fragment totals are sticky)
+  cudaMemsetAsync(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 0, 5 * 4, s);
+  return cuda_err(cudaGetLastError());
+}
+
+SwrTargetDesc make_target(const swr_context* c) {
+  SwrTargetDesc T;
+  memset(&T, 0, sizeof(T));
+  T.width = c->u.width;
+  T.height = c->u.height;
+  T.tiles_x = (T.width + c->tile - 1) / c->tile;
+  T.tiles_y = (T.height + c->tile - 1) / c->tile;
+  T.tile_base = 0;
+  T.first_draw = 0;
+  return T;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swr_create(swr_context** out) {
+  if (!out) return SWR_EINVAL;
+  swr_context* c = new swr_context();
+  memset(&c->u, 0, sizeof(c->u));
+  if (!c->status.ensure(kStatusWords * 4)) {
+    delete c;
+    return SWR_ENOMEM;
+  }
+  if (cudaMemset(c->status.p, 0, kStatusWords * 4) != cudaSuccess ||
+      cudaMallocHost((void**)&c->status_host, kStatusWords * 4) != cudaSuccess) {
+    delete c;
+    return SWR_ECUDA;
+  }
+  *out = c;
+  return SWR_OK;
+}
+
+int swr_destroy(swr_context* c) {
+  if (!c) return SWR_EINVAL;
+  if (c->status_host) cudaFreeHost(c->status_host);
+  delete c;
+  return SWR_OK;
+}
+
+int swr_set_viewport(swr_context* c, int x, int y, int w, int h) {
+  if (!c) return SWR_EINVAL;
+  c->vp_x = x; c->vp_y = y; c->vp_w = w; c->vp_h = h;
+  return SWR_OK;
+}
+
+int swr_set_depth_range(swr_context* c, float n, float f) {
+  if (!c) return SWR_EINVAL;
+  c->dn = n; c->df = f;
+  return SWR_OK;
+}
+
+int swr_set_cull_mode(swr_context* c, int mode) {
+  if (!c || mode < 0 || mode > 2) return SWR_EINVAL;
+  c->cull = mode;
+  return SWR_OK;
+}
+
+int swr_set_vertex_shader(swr_context* c, int id) {
+  if (!c || !vs_ops(id)) return SWR_EINVAL;
+  c->vs_id = id;
+  return SWR_OK;
+}
+
+int swr_set_vertex_attrib_pointer(swr_context* c, int index, int stride, const void* buffer, uint64_t bytes) {
+  if (!c || index < 0 || index >= 8 || stride < 0) return SWR_EINVAL;  // VertexProcessor.cpp:69
+  c->attribs[index].ptr = buffer;
+  c->attribs[index].stride = stride;
+  c->attribs[index].bytes = bytes;
+  return SWR_OK;
+}
+
+int swr_set_raster_mode(swr_context* c, int mode) {
+  if (!c || mode < 0 || mode > 2) return SWR_EINVAL;
+  c->raster_mode = mode;
+  return SWR_OK;
+}
+
+int swr_set_scissor_rect(swr_context* c, int x, int y, int w, int h) {
+  if (!c) return SWR_EINVAL;
+  c->sc_x = x; c->sc_y = y; c->sc_w = w; c->sc_h = h;
+  return SWR_OK;
+}
+
+int swr_set_pixel_shader(swr_context* c, int id) {
+  if (!c || !ps_ops(id)) return SWR_EINVAL;
+  c->ps_id = id;
+  return SWR_OK;
+}
+
+int swr_set_uniforms(swr_context* c, const SwrUniforms* u) {
+  if (!c || !u || u->width <= 0 || u->height <= 0 || !u->color) return SWR_EINVAL;
+  c->u = *u;
+  c->have_u = true;
+  return SWR_OK;
+}
+
+int swr_set_tile_size(swr_context* c, int tile) {
+  if (!c || (tile != 16 && tile != 32)) return SWR_EINVAL;
+  c->tile = tile;
+  return SWR_OK;
+}
+
+int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* indices, void* stream) {
+  if (!c || !c->have_u) return SWR_EINVAL;
+  const VsOps* vs = vs_ops(c->vs_id);
+  const PsOps* ps = ps_ops(c->ps_id);
+  if (!vs || !ps) return SWR_EINVAL;
+  if (mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // points and lines: see swr_lines.cu
+  if (count % 3 || count / 3 >= 0x7fffffffull || (count && !indices)) return SWR_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint64_t nverts = ~0ull;
+  for (int a = 0; a < vs->attribs; ++a) {
+    const Attrib& at = c->attribs[a];
+    const uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
+    if (!at.ptr || at.stride <= 0 || at.bytes == 0) return SWR_EINVAL;
+    // element i occupies [i * stride, i * stride + elem): the last one must fit
+    const uint64_t n = at.bytes >= elem ? (at.bytes - elem) / (uint64_t)at.stride + 1 : 0;
+    nverts = n < nverts ? n : nverts;
+  }
+  if (vs->attribs == 0) nverts = 0;
+  if (nverts >= 0x7fffffffull) return SWR_EINVAL;
+  const uint32_t nsub = (uint32_t)(count / 3);
+  const uint32_t nbatches = (nsub + SWR_BATCH_PRIMS - 1) / SWR_BATCH_PRIMS;
+  const SwrTargetDesc T = make_target(c);
+  const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
+  int rc = ensure_capacity(c, (uint32_t)nverts, vs->S, nsub, nbatches, ntiles, ps->R);
+  if (rc) return rc;
+  SwrDrawDesc D;
+  fill_draw(c, D, mode);
+  D.indices = indices;
+  D.nidx = (uint32_t)count;
+  D.nverts = (uint32_t)nverts;
+  D.nprims = nsub;
+  if ((rc = upload_single(c, D, T, s))) return rc;
+  uint32_t* st = c->status.as<uint32_t>();
+  vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts, c->ptv.as<float>(), s);
+  AssembleArgs aa;
+  aa.draws = c->draws.as<SwrDrawDesc>();
+  aa.ndraws = 1;
+  aa.draw_bbase = c->draw_bbase.as<uint32_t>();
+  aa.ptv = c->ptv.as<float>();
+  aa.clipv = c->clipv.as<float>();
+  aa.clip_table = c->clip_table.as<SwrClipEntry>();
+  aa.clip_slot = c->clip_slot.as<uint32_t>();
+  aa.tri_flags = c->tri_flags.as<uint8_t>();
+  aa.batch_counts = c->batch_counts.as<uint2>();
+  aa.batch_base = c->batch_base.as<uint32_t>();
+  aa.tris = c->tris.as<uint4>();
+  aa.status = st;
+  aa.cap_clip_slots = c->cap_clip_slots;
+  aa.cap_clip_verts = c->cap_clip_verts;
+  aa.cap_prims = c->cap_prims;
+  vs->assemble_count(aa, nbatches, s);
+  k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
+                                  c->cap_prims);
+  vs->assemble_emit(aa, nbatches, s);
+  c->last_ntiles = ntiles;
+  return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s);
+}
+
+int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nverts, const int32_t* indices,
+                  uint64_t count, void* stream) {
+  if (!c || !c->have_u) return SWR_EINVAL;
+  const PsOps* ps = ps_ops(c->ps_id);
+  if (!ps) return SWR_EINVAL;
+  if (mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;
+  if (count % 3 || count / 3 >= 0x7fffffffull || nverts >= 0x7fffffffull) return SWR_EINVAL;
+  if ((count && !indices) || (nverts && !vertices)) return SWR_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t nsub = (uint32_t)(count / 3);
+  const SwrTargetDesc T = make_target(c);
+  const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
+  int rc = ensure_capacity(c, (uint32_t)nverts, ps->S, nsub, 1, ntiles, ps->R);
+  if (rc) return rc;
+  if (!c->direct_keep.ensure((size_t)nsub * 4 + 16) || !c->direct_pos.ensure((size_t)nsub * 4 + 16))
+    return SWR_ENOMEM;
+  SwrDrawDesc D;
+  fill_draw(c, D, mode);
+  D.direct = 1;
+  D.nprims = nsub;
+  D.nverts = (uint32_t)nverts;
+  if ((rc = upload_single(c, D, T, s))) return rc;
+  uint32_t* st = c->status.as<uint32_t>();
+  ps->direct_vertices(vertices, (uint32_t)nverts, c->ptv.as<float>(), s);
+  if (nsub) {
+    const int grid = (int)((nsub + 255) / 256 < 1216 ? (nsub + 255) / 256 : 1216);
+    k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, 3, c->direct_keep.as<uint32_t>());
+    scan_exclusive(c->direct_keep.as<uint32_t>(), c->direct_pos.as<uint32_t>(), nullptr, nsub,
+                   st + SWR_ST_PRIMS, c->scratch.as<uint32_t>(), s);
+    k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, 3, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
+                                       c->direct_pos.as<uint32_t>(), c->tris.as<uint4>(), st);
+  }
+  c->last_ntiles = ntiles;
+  return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s);
+}
+
+int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
+  if (!c) return SWR_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = cuda_err(cudaMemcpyAsync(c->status_host, c->status.p, kStatusWords * 4, cudaMemcpyDeviceToHost, s));
+  if (rc) return rc;
+  if ((rc = cuda_err(cudaStreamSynchronize(s)))) return rc;
+  const uint32_t* h = c->status_host;
+  if (stats) {
+    stats->fragments = (uint64_t)h[SWR_ST_SHADED_LO] | ((uint64_t)h[SWR_ST_SHADED_HI] << 32);
+    stats->primitives = h[SWR_ST_PRIMS];
+    stats->bin_pairs = h[SWR_ST_PAIRS];
+    stats->clip_polygons = h[SWR_ST_CLIP_SLOTS];
+    stats->flags = h[SWR_ST_FLAGS];
+  }
+  const uint32_t flags = h[SWR_ST_FLAGS];
+  if (flags & SWR_F_ANY_OVERFLOW) {
+    grow_u32(c->cap_clip_slots, h[kStickyBase + SWR_ST_CLIP_SLOTS]);
+    grow_u32(c->cap_clip_verts, h[kStickyBase + SWR_ST_CLIP_VERTS]);
+    grow_u32(c->cap_prims, h[kStickyBase + SWR_ST_PRIMS]);
+    grow_u32(c->cap_pairs, h[kStickyBase + SWR_ST_PAIRS]);
+  }
+  cudaMemsetAsync(c->status.p, 0, kStatusWords * 4, s);
+  if ((rc = cuda_err(cudaStreamSynchronize(s)))) return rc;
+  if (flags & SWR_F_ANY_OVERFLOW) return SWR_EOVERFLOW;
+  if (flags & SWR_F_BAD_INDEX) return SWR_EINDEX;
+  return SWR_OK;
+}
+
+const char* swr_status_string(int st) {
+  switch (st) {
+    case SWR_OK: return "ok";
+    case SWR_EINVAL: return "invalid argument";
+    case SWR_ENOMEM: return "out of device memory";
+    case SWR_EOVERFLOW: return "scratch queue overflow (queue grown; issue the draw again)";
+    case SWR_ECUDA: return "CUDA error";
+    case SWR_EINDEX: return "index beyond the bound vertex buffers";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

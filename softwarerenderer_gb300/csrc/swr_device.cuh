@@ -1,0 +1,115 @@
+// Device-side data structures and small collective helpers of the GB300 pipeline.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "swr_programs.h"
+
+#define SWR_BATCH_PRIMS 1024  // VertexProcessor flushes every 1024 primitives (VertexProcessor.cpp:110-116)
+#define SWR_BLOCK 8           // swr::BlockSize (IRasterizer.h:33)
+#define SWR_CLIP_REF 0x80000000u  // vertex references with this bit address the clip-vertex buffer
+
+// Status word layout (device memory, reset by every submission).
+enum SwrStatusWord {
+  SWR_ST_FLAGS = 0,       // error bits, see SwrStatusFlags
+  SWR_ST_CLIP_SLOTS = 1,  // clip-table entries requested
+  SWR_ST_CLIP_VERTS = 2,  // clip vertices requested
+  SWR_ST_PRIMS = 3,       // primitives after clipping and culling
+  SWR_ST_PAIRS = 4,       // (tile, primitive) pairs requested
+  SWR_ST_FRAGS = 5,       // line/point fragments requested
+  SWR_ST_SHADED_LO = 6,   // drawPixel calls (64-bit, low word)
+  SWR_ST_SHADED_HI = 7,
+  SWR_ST_WORDS = 8
+};
+
+enum SwrStatusFlags {
+  SWR_F_BAD_INDEX = 1,       // an index addressed a vertex beyond the attribute buffers
+  SWR_F_CLIP_OVERFLOW = 2,   // clip table or clip-vertex buffer too small
+  SWR_F_PRIM_OVERFLOW = 4,   // primitive buffer too small
+  SWR_F_PAIR_OVERFLOW = 8,   // bin pair buffer too small
+  SWR_F_FRAG_OVERFLOW = 16,  // line/point fragment buffer too small
+  SWR_F_CLIP_COMPLEX = 32,   // a clipped polygon exceeded 16 vertices and was dropped
+};
+#define SWR_F_ANY_OVERFLOW (SWR_F_CLIP_OVERFLOW | SWR_F_PRIM_OVERFLOW | SWR_F_PAIR_OVERFLOW | SWR_F_FRAG_OVERFLOW)
+
+// One draw of a submission: the state VertexProcessor and Rasterizer hold for one
+// drawElements call (VertexProcessor.h:140-151, Rasterizer.h:54-63).
+struct SwrDrawDesc {
+  const void* attrib[8];
+  int32_t attrib_stride[8];
+  const uint32_t* indices;
+  uint32_t nidx;      // index count
+  uint32_t nverts;    // vertices addressable in every bound attribute stream
+  uint32_t vbase;     // first post-transform vertex of this draw
+  uint32_t pbase;     // first submitted primitive of this draw (global numbering)
+  uint32_t bbase;     // first batch of this draw (global numbering)
+  uint32_t nprims;    // submitted primitives
+  int32_t target;     // render target index
+  int32_t draw_mode;  // 0 Point, 1 Line, 2 Triangle
+  int32_t cull;       // 0 None, 1 CCW, 2 CW
+  int32_t raster_mode;  // 0 Span, 1 Block, 2 Adaptive
+  float vp_px, vp_py, vp_ox, vp_oy;  // VertexProcessor::setViewport (VertexProcessor.cpp:43-54)
+  float dn, df;                      // VertexProcessor::setDepthRange
+  int32_t sc_minx, sc_miny, sc_maxx, sc_maxy;  // Rasterizer::setScissorRect (Rasterizer.h:81-87)
+  int32_t direct;     // 1: vertices are RasterizerVertex records already in screen space
+  int32_t _pad;
+  SwrUniforms u;
+};
+
+// Render target: a tile grid over width x height pixels.  Draws that share a target
+// share its tiles, so their primitives meet in one ordered bin per tile.
+struct SwrTargetDesc {
+  int32_t width, height;
+  int32_t tiles_x, tiles_y;
+  uint32_t tile_base;
+  int32_t first_draw;  // draw whose uniforms carry the framebuffer pointers
+  int32_t _pad[2];
+};
+
+// Result of clipping one triangle (PolyClipper, PolyClipper.cpp:45-81): a polygon of up
+// to 16 vertices emitted as a fan; keep/swap bits per fan triangle from culling.
+struct SwrClipEntry {
+  uint32_t ref[16];
+  uint16_t n;
+  uint16_t keep;
+  uint16_t swap;
+  uint16_t _pad;
+};
+
+// Index of the last element of sorted `base[0..n)` that is <= key.
+__device__ __forceinline__ int swr_find_le(const uint32_t* base, int n, uint32_t key) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= key) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x multiple of 32, <= 1024).
+// `tmp` needs 32 words.  Returns the exclusive prefix; *total receives the block sum.
+__device__ __forceinline__ uint32_t swr_block_exscan(uint32_t v, uint32_t* tmp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) tmp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < nwarps ? tmp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    tmp[lane] = s;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t warp_off = warp ? tmp[warp - 1] : 0u;
+  if (total) *total = tmp[nwarps - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}

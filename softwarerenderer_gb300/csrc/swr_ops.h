@@ -1,0 +1,32 @@
+// Per-program stage launchers: the host side of setVertexShader<VS> / setPixelShader<PS>
+// (VertexProcessor.h:77-85, Rasterizer.h:90-96).  Each built-in shader is compiled into
+// its own kernels; the context picks the launchers by program id.
+#pragma once
+#include "swr_stages.cuh"
+
+namespace swr {
+
+struct VsOps {
+  int attribs, A, P, S;  // AttribCount, AVarCount, PVarCount, post-transform record stride
+  int elem_bytes[2];     // bytes read per element of attribute streams 0 and 1
+  void (*vertex)(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase, uint32_t nverts,
+                 float* ptv, cudaStream_t s);
+  void (*assemble_count)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
+  void (*assemble_emit)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
+};
+
+struct PsOps {
+  int A, P, R, S;  // AVarCount, PVarCount, setup record words, direct-path vertex stride
+  void (*direct_vertices)(const float* rv, uint32_t n, float* ptv, cudaStream_t s);
+  void (*setup)(const SetupArgs& a, cudaStream_t s);
+  void (*emit_pairs)(const uint32_t* status, uint32_t cap_prims, const float* recs,
+                     const uint32_t* tile_count, const uint32_t* pair_off, const uint32_t* npairs,
+                     uint32_t cap_pairs, const SwrDrawDesc* draws, const SwrTargetDesc* targets,
+                     int tile, uint32_t* keys, uint32_t* vals, uint32_t* status_w, cudaStream_t s);
+  void (*raster)(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s);
+};
+
+const VsOps* vs_ops(int id);
+const PsOps* ps_ops(int id);
+
+}  // namespace swr

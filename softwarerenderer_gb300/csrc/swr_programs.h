@@ -6,7 +6,8 @@
 // FMA, correctly rounded divide and square root only).
 //
 // Vertex shader contract (mirrors VertexShaderBase): static AttribCount, AVarCount,
-// PVarCount and processVertex(in, out, uniforms) where in[i] points at element
+// PVarCount, the bytes read from each attribute element (Bytes0, Bytes1) and
+// processVertex(in, out, uniforms) where in[i] points at element
 // `index` of attribute stream i (VertexProcessor::attribPointer,
 // VertexProcessor.cpp:134-139) and out exposes x, y, z, w, avar[], pvar[].
 //
@@ -71,7 +72,7 @@ SWR_HD float swr_u8_channel(uint32_t c, int sh) { return (float)((c >> sh) & 0xf
 
 // Textured mesh: stream 0 = {x, y, z, u, v} (20 B).  PVar = uv.
 struct VsPosUV {
-  enum { AttribCount = 1, AVarCount = 0, PVarCount = 2 };
+  enum { AttribCount = 1, AVarCount = 0, PVarCount = 2, Bytes0 = 20, Bytes1 = 0 };
   template <class Out>
   SWR_HD static void processVertex(const SwrVertexInput& in, Out* out, const SwrUniforms& u) {
     const float* d = (const float*)in.p[0];
@@ -86,7 +87,7 @@ struct VsPosUV {
 // Lit mesh: stream 0 = {x, y, z, nx, ny, nz} (24 B), stream 1 = {u, v} (8 B).
 // AVar = normal, PVar = uv.
 struct VsPosNrmUV {
-  enum { AttribCount = 2, AVarCount = 3, PVarCount = 2 };
+  enum { AttribCount = 2, AVarCount = 3, PVarCount = 2, Bytes0 = 24, Bytes1 = 8 };
   template <class Out>
   SWR_HD static void processVertex(const SwrVertexInput& in, Out* out, const SwrUniforms& u) {
     const float* d = (const float*)in.p[0];
@@ -101,7 +102,7 @@ struct VsPosNrmUV {
 
 // Vertex colour, perspective-correct: stream 0 = {x, y, z, r, g, b} (24 B).  PVar = rgb.
 struct VsPosRGB {
-  enum { AttribCount = 1, AVarCount = 0, PVarCount = 3 };
+  enum { AttribCount = 1, AVarCount = 0, PVarCount = 3, Bytes0 = 24, Bytes1 = 0 };
   template <class Out>
   SWR_HD static void processVertex(const SwrVertexInput& in, Out* out, const SwrUniforms& u) {
     const float* d = (const float*)in.p[0];
@@ -115,7 +116,7 @@ struct VsPosRGB {
 // Vertex colour, affine: stream 0 = {x, y, z, r, g, b} (24 B).  AVar = rgb.  With an
 // identity mvp this is the vertex shader of Benchmark.cpp:32-49 / VertexProcessorTest.
 struct VsPosRGBAffine {
-  enum { AttribCount = 1, AVarCount = 3, PVarCount = 0 };
+  enum { AttribCount = 1, AVarCount = 3, PVarCount = 0, Bytes0 = 24, Bytes1 = 0 };
   template <class Out>
   SWR_HD static void processVertex(const SwrVertexInput& in, Out* out, const SwrUniforms& u) {
     const float* d = (const float*)in.p[0];
@@ -129,7 +130,7 @@ struct VsPosRGBAffine {
 // Differentiable-rendering mesh: stream 0 = {x, y, z, r, g, b, u, v} (32 B).
 // PVar = {r, g, b, u, v}.
 struct VsPosRGBUV {
-  enum { AttribCount = 1, AVarCount = 0, PVarCount = 5 };
+  enum { AttribCount = 1, AVarCount = 0, PVarCount = 5, Bytes0 = 32, Bytes1 = 0 };
   template <class Out>
   SWR_HD static void processVertex(const SwrVertexInput& in, Out* out, const SwrUniforms& u) {
     const float* d = (const float*)in.p[0];

@@ -1,0 +1,74 @@
+// Raster-stage kernels of the built-in pixel shaders.
+#include "swr_ops.h"
+
+namespace swr {
+namespace {
+
+constexpr int kGrid = 152 * 8;
+constexpr int kChunk = 64;  // primitives staged in shared memory per bin chunk
+
+template <class PS>
+void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {
+  if (!n) return;
+  const uint32_t want = (n + 255) / 256;
+  const int grid = (int)(want < (uint32_t)kGrid ? want : (uint32_t)kGrid);
+  k_direct_vertices<PS::AVarCount, PS::PVarCount><<<grid, 256, 0, s>>>(rv, n, ptv);
+}
+
+template <class PS>
+void run_setup(const SetupArgs& a, cudaStream_t s) {
+  k_setup<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+void run_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+               const uint32_t* pair_off, const uint32_t* npairs, uint32_t cap_pairs,
+               const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* keys,
+               uint32_t* vals, uint32_t* status_w, cudaStream_t s) {
+  k_emit_pairs<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, pair_off, npairs, cap_pairs,
+                                         draws, targets, tile, keys, vals, status_w);
+}
+
+template <class PS>
+void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
+  if (!ntiles) return;
+  if (tile == 32) k_raster<PS, 32, kChunk><<<ntiles, 256, 0, s>>>(a);
+  else k_raster<PS, 16, kChunk><<<ntiles, 256, 0, s>>>(a);
+}
+
+template <class PS>
+PsOps make() {
+  PsOps o;
+  o.A = PS::AVarCount;
+  o.P = PS::PVarCount;
+  o.R = Rec<PS>::R;
+  o.S = VLayout<PS::AVarCount, PS::PVarCount>::S;
+  o.direct_vertices = &run_direct<PS>;
+  o.setup = &run_setup<PS>;
+  o.emit_pairs = &run_pairs<PS>;
+  o.raster = &run_raster<PS>;
+  return o;
+}
+
+const PsOps kTexNearest = make<PsTexNearest>();
+const PsOps kLambert = make<PsLambert>();
+const PsOps kVColor = make<PsVColor>();
+const PsOps kVColorAffine = make<PsVColorAffine>();
+const PsOps kLambertTex = make<PsLambertTex>();
+const PsOps kDiff = make<PsDiff>();
+
+}  // namespace
+
+const PsOps* ps_ops(int id) {
+  switch (id) {
+    case SWR_PS_TEX_NEAREST: return &kTexNearest;
+    case SWR_PS_LAMBERT: return &kLambert;
+    case SWR_PS_VCOLOR: return &kVColor;
+    case SWR_PS_VCOLOR_AFFINE: return &kVColorAffine;
+    case SWR_PS_LAMBERT_TEX: return &kLambertTex;
+    case SWR_PS_DIFF: return &kDiff;
+    default: return nullptr;
+  }
+}
+
+}  // namespace swr

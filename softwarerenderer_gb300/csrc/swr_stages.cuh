@@ -1,0 +1,887 @@
+// Pipeline stages of the GB300 rasterizer, templated on the shader programs.
+//
+//   k_vertex          VertexShader::processVertex once per vertex + outcodes + divide and
+//                     viewport (VertexProcessor.cpp:122-150, :347-377)
+//   k_assemble_count  one CTA per 1024-primitive batch: outcode OR, polygon clipping
+//                     (PolyClipper.cpp:45-81), fan split and culling (VertexProcessor.cpp:
+//                     217-263, :319-345); counts survivors per batch
+//   k_assemble_emit   writes the surviving triangles in the reference's effective order:
+//                     per batch, the input slots in order, then every extra fan triangle
+//                     in parent order (VertexProcessor.cpp:254-260)
+//   k_setup           TriangleEquations (TriangleEquations.h:47-71) and the raster-mode
+//                     decision, bounding boxes and tile counts per primitive
+//   k_emit_pairs      (tile, primitive) pairs in primitive order -> stable radix sort
+//   k_raster          one CTA per screen tile; each thread owns pixels and walks the
+//                     tile's bin in primitive order, reproducing Span (Rasterizer.h:309-411)
+//                     and Block (Rasterizer.h:225-306, PixelShaderBase.h:55-112) coverage
+//                     and incrementally stepped interpolants exactly, then calls the pixel
+//                     shader in the same per-pixel order as the reference.
+//
+// All arithmetic on the parity path uses the _rn intrinsics (no FMA contraction).
+#pragma once
+#include "swr_device.cuh"
+#include "swr_math.h"
+
+namespace swr {
+
+// ---------------------------------------------------------------------------------
+// Post-transform vertex record (floats): 0-3 clip x,y,z,w | 4-6 screen x,y,z | 7 outcode
+// | 8.. avar[A] | pvar[P].  Stride rounded to 16 bytes.
+template <int A, int P>
+struct VLayout {
+  enum { NA = A, NP = P, OFF_A = 8, OFF_P = 8 + A, S = ((8 + A + P + 3) / 4) * 4 };
+};
+
+template <int A, int P>
+struct VsOut {
+  float x, y, z, w;
+  float avar[A > 0 ? A : 1];
+  float pvar[P > 0 ? P : 1];
+};
+
+__device__ __forceinline__ int outcode(float x, float y, float z, float w) {
+  // VertexProcessor::clipMask (VertexProcessor.cpp:122-132)
+  int m = 0;
+  if (swr_sub(w, x) < 0.0f) m |= 0x01;
+  if (swr_add(x, w) < 0.0f) m |= 0x02;
+  if (swr_sub(w, y) < 0.0f) m |= 0x04;
+  if (swr_add(y, w) < 0.0f) m |= 0x08;
+  if (swr_sub(w, z) < 0.0f) m |= 0x10;
+  if (swr_add(z, w) < 0.0f) m |= 0x20;
+  return m;
+}
+
+// Perspective divide, viewport and depth range (VertexProcessor.cpp:364-373).
+__device__ __forceinline__ void to_screen(const SwrDrawDesc& D, float x, float y, float z, float w,
+                                          float& sx, float& sy, float& sz) {
+  const float iw = swr_div(1.0f, w);
+  const float nx = swr_mul(x, iw), ny = swr_mul(y, iw), nz = swr_mul(z, iw);
+  sx = swr_add(swr_mul(D.vp_px, nx), D.vp_ox);
+  sy = swr_add(swr_mul(D.vp_py, -ny), D.vp_oy);
+  sz = swr_add(swr_mul(swr_mul(0.5f, swr_sub(D.df, D.dn)), nz), swr_mul(0.5f, swr_add(D.dn, D.df)));
+}
+
+template <class VS>
+__global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ draws, int ndraws,
+                                                const uint32_t* __restrict__ draw_vbase,
+                                                uint32_t nverts, float* __restrict__ ptv) {
+  typedef VLayout<VS::AVarCount, VS::PVarCount> L;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nverts; v += gridDim.x * blockDim.x) {
+    const int d = ndraws > 1 ? swr_find_le(draw_vbase, ndraws, v) : 0;
+    const SwrDrawDesc& D = draws[d];
+    const uint32_t local = v - D.vbase;
+    SwrVertexInput in;
+#pragma unroll
+    for (int a = 0; a < VS::AttribCount; ++a)
+      in.p[a] = (const char*)D.attrib[a] + (size_t)D.attrib_stride[a] * (size_t)local;
+    VsOut<VS::AVarCount, VS::PVarCount> o;
+    VS::processVertex(in, &o, D.u);
+    float rec[L::S];
+    rec[0] = o.x; rec[1] = o.y; rec[2] = o.z; rec[3] = o.w;
+    to_screen(D, o.x, o.y, o.z, o.w, rec[4], rec[5], rec[6]);
+    rec[7] = __int_as_float(outcode(o.x, o.y, o.z, o.w));
+#pragma unroll
+    for (int i = 0; i < VS::AVarCount; ++i) rec[L::OFF_A + i] = o.avar[i];
+#pragma unroll
+    for (int i = 0; i < VS::PVarCount; ++i) rec[L::OFF_P + i] = o.pvar[i];
+#pragma unroll
+    for (int i = 8 + VS::AVarCount + VS::PVarCount; i < L::S; ++i) rec[i] = 0.0f;
+    float4* dst = (float4*)(ptv + (size_t)v * L::S);
+#pragma unroll
+    for (int i = 0; i < L::S / 4; ++i) dst[i] = make_float4(rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]);
+  }
+}
+
+// Direct Rasterizer path: RasterizerVertex (x, y, z, w, avar[16], pvar[16]) records are
+// already in screen space; convert them to the post-transform layout of the pixel shader.
+template <int A, int P>
+__global__ void k_direct_vertices(const float* __restrict__ rv, uint32_t nverts, float* __restrict__ ptv) {
+  typedef VLayout<A, P> L;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nverts; v += gridDim.x * blockDim.x) {
+    const float* s = rv + (size_t)v * 36;
+    float* o = ptv + (size_t)v * L::S;
+    o[0] = s[0]; o[1] = s[1]; o[2] = s[2]; o[3] = s[3];
+    o[4] = s[0]; o[5] = s[1]; o[6] = s[2]; o[7] = __int_as_float(0);
+    for (int i = 0; i < A; ++i) o[L::OFF_A + i] = s[4 + i];
+    for (int i = 0; i < P; ++i) o[L::OFF_P + i] = s[20 + i];
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Triangle assembly, clipping and culling.
+
+// Polygon clipper over a per-thread vertex pool (clip-space x,y,z,w + A + P values).
+// A convex cut adds one vertex per plane (at most 9 in total); exact zeros in the plane
+// distances can add more, so both the polygon and the pool are bounds-checked and a
+// polygon that would exceed them is reported (SWR_F_CLIP_COMPLEX) and dropped.
+template <int A, int P>
+struct Clipper {
+  enum { NV = 4 + A + P, POOL = 24, MAXPOLY = 16 };
+  float pool[POOL][NV];
+  int npool;
+  int poly[MAXPOLY + 1];
+  int npoly;
+  bool bad;
+
+  __device__ void lerp(int i0, int i1, float t) {  // Helper::interpolateVertex (PolyClipper.h:34-48)
+    const float s = swr_sub(1.0f, t);
+    float* r = pool[npool];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) r[k] = swr_add(swr_mul(pool[i0][k], s), swr_mul(pool[i1][k], t));
+    npool++;
+  }
+
+  __device__ static float dist(const float* v, float a, float b, float c, float d) {
+    return swr_add(swr_add(swr_add(swr_mul(a, v[0]), swr_mul(b, v[1])), swr_mul(c, v[2])), swr_mul(d, v[3]));
+  }
+
+  __device__ static int sgn(float v) { return (0.0f < v) - (v < 0.0f); }
+
+  // PolyClipper::clipToPlane (PolyClipper.cpp:45-81).
+  __device__ void clip(float a, float b, float c, float d) {
+    if (npoly < 3 || bad) return;
+    int out[MAXPOLY + 1];
+    int nout = 0;
+    int iprev = poly[0];
+    poly[npoly] = iprev;
+    float dprev = dist(pool[iprev], a, b, c, d);
+    for (int i = 1; i <= npoly; ++i) {
+      const int icur = poly[i];
+      const float dcur = dist(pool[icur], a, b, c, d);
+      if (dprev >= 0.0f) {
+        if (nout >= MAXPOLY) { bad = true; return; }
+        out[nout++] = iprev;
+      }
+      if (sgn(dcur) != sgn(dprev)) {
+        if (nout >= MAXPOLY || npool >= POOL) { bad = true; return; }
+        const float t = dcur < 0.0f ? swr_div(dprev, swr_sub(dprev, dcur))
+                                    : swr_div(-dprev, swr_sub(dcur, dprev));
+        lerp(iprev, icur, t);
+        out[nout++] = npool - 1;
+      }
+      iprev = icur;
+      dprev = dcur;
+    }
+    for (int i = 0; i < nout; ++i) poly[i] = out[i];
+    npoly = nout;
+  }
+};
+
+// facing test of VertexProcessor::cullTriangles (VertexProcessor.cpp:330-343):
+// returns 0 = drop, 1 = keep, 3 = keep and swap v0 <-> v2.
+__device__ __forceinline__ int cull_decision(int cull, float x0, float y0, float x1, float y1,
+                                             float x2, float y2) {
+  const float facing = swr_sub(swr_mul(swr_sub(x0, x1), swr_sub(y2, y1)),
+                               swr_mul(swr_sub(x2, x1), swr_sub(y0, y1)));
+  if (facing < 0.0f) return cull == 2 ? 0 : 1;
+  return cull == 1 ? 0 : 3;
+}
+
+struct AssembleArgs {
+  const SwrDrawDesc* draws;
+  int ndraws;
+  const uint32_t* draw_bbase;
+  const float* ptv;
+  float* clipv;             // clip-generated vertices (post-transform layout)
+  SwrClipEntry* clip_table;
+  uint32_t* clip_slot;      // per submitted primitive (valid when clipped)
+  uint8_t* tri_flags;       // per submitted primitive: bit0 keep, bit1 swap, bit2 clipped
+  uint2* batch_counts;      // per batch: (kept input slots, kept extra fan triangles)
+  const uint32_t* batch_base;
+  uint4* tris;              // output primitives: v0, v1, v2 references + draw id
+  uint32_t* status;
+  uint32_t cap_clip_slots, cap_clip_verts, cap_prims;
+};
+
+template <int A, int P>
+__device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, int d, uint32_t p,
+                             uint32_t& in_kept, uint32_t& ex_kept) {
+  typedef VLayout<A, P> L;
+  in_kept = ex_kept = 0;
+  const uint32_t gp = D.pbase + p;
+  const uint32_t i0 = D.indices[3 * p], i1 = D.indices[3 * p + 1], i2 = D.indices[3 * p + 2];
+  if (i0 >= D.nverts || i1 >= D.nverts || i2 >= D.nverts) {
+    atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_BAD_INDEX);
+    g.tri_flags[gp] = 0;
+    return;
+  }
+  const uint32_t r[3] = {D.vbase + i0, D.vbase + i1, D.vbase + i2};
+  const float* v[3] = {g.ptv + (size_t)r[0] * L::S, g.ptv + (size_t)r[1] * L::S, g.ptv + (size_t)r[2] * L::S};
+  const int m = __float_as_int(v[0][7]) | __float_as_int(v[1][7]) | __float_as_int(v[2][7]);
+  if (m == 0) {
+    const int c = cull_decision(D.cull, v[0][4], v[0][5], v[1][4], v[1][5], v[2][4], v[2][5]);
+    g.tri_flags[gp] = (uint8_t)c;
+    in_kept = c & 1;
+    return;
+  }
+  // Clip in the reference's plane order +X, -X, +Y, -Y, +Z, -Z (VertexProcessor.cpp:237-242).
+  Clipper<A, P> cp;
+  for (int k = 0; k < 3; ++k) {
+    cp.pool[k][0] = v[k][0]; cp.pool[k][1] = v[k][1]; cp.pool[k][2] = v[k][2]; cp.pool[k][3] = v[k][3];
+    for (int i = 0; i < A; ++i) cp.pool[k][4 + i] = v[k][L::OFF_A + i];
+    for (int i = 0; i < P; ++i) cp.pool[k][4 + A + i] = v[k][L::OFF_P + i];
+    cp.poly[k] = k;
+  }
+  cp.npool = 3;
+  cp.npoly = 3;
+  cp.bad = false;
+  if (m & 0x01) cp.clip(-1.0f, 0.0f, 0.0f, 1.0f);
+  if (m & 0x02) cp.clip(1.0f, 0.0f, 0.0f, 1.0f);
+  if (m & 0x04) cp.clip(0.0f, -1.0f, 0.0f, 1.0f);
+  if (m & 0x08) cp.clip(0.0f, 1.0f, 0.0f, 1.0f);
+  if (m & 0x10) cp.clip(0.0f, 0.0f, -1.0f, 1.0f);
+  if (m & 0x20) cp.clip(0.0f, 0.0f, 1.0f, 1.0f);
+  if (cp.bad) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_CLIP_COMPLEX);
+  if (cp.npoly < 3 || cp.bad) {
+    g.tri_flags[gp] = 4;  // clipped away entirely
+    g.clip_slot[gp] = 0xffffffffu;
+    return;
+  }
+  // Screen positions of the polygon (generated vertices are transformed here).
+  float sx[Clipper<A, P>::MAXPOLY], sy[Clipper<A, P>::MAXPOLY], sz[Clipper<A, P>::MAXPOLY];
+  int nnew = 0;
+  for (int k = 0; k < cp.npoly; ++k) {
+    const int pi = cp.poly[k];
+    if (pi < 3) {
+      sx[k] = v[pi][4]; sy[k] = v[pi][5]; sz[k] = v[pi][6];
+    } else {
+      to_screen(D, cp.pool[pi][0], cp.pool[pi][1], cp.pool[pi][2], cp.pool[pi][3], sx[k], sy[k], sz[k]);
+      nnew++;
+    }
+  }
+  uint32_t keep = 0, swap = 0;  // bit k: fan triangle (p0, p[k+1], p[k+2])
+  for (int k = 0; k + 2 < cp.npoly; ++k) {
+    const int c = cull_decision(D.cull, sx[0], sy[0], sx[k + 1], sy[k + 1], sx[k + 2], sy[k + 2]);
+    if (c & 1) keep |= 1u << k;
+    if (c & 2) swap |= 1u << k;
+  }
+  const uint32_t slot = atomicAdd(&g.status[SWR_ST_CLIP_SLOTS], 1u);
+  const uint32_t vb = atomicAdd(&g.status[SWR_ST_CLIP_VERTS], (uint32_t)nnew);
+  if (slot >= g.cap_clip_slots || vb + nnew > g.cap_clip_verts) {
+    atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_CLIP_OVERFLOW);
+    g.tri_flags[gp] = 4;
+    g.clip_slot[gp] = 0xffffffffu;
+    return;
+  }
+  SwrClipEntry ent;
+  int nv = 0;
+  for (int k = 0; k < cp.npoly; ++k) {
+    const int pi = cp.poly[k];
+    if (pi < 3) {
+      ent.ref[k] = r[pi];
+    } else {
+      const uint32_t id = vb + nv++;
+      float* o = g.clipv + (size_t)id * L::S;
+      o[0] = cp.pool[pi][0]; o[1] = cp.pool[pi][1]; o[2] = cp.pool[pi][2]; o[3] = cp.pool[pi][3];
+      o[4] = sx[k]; o[5] = sy[k]; o[6] = sz[k]; o[7] = __int_as_float(0);
+      for (int i = 0; i < A; ++i) o[L::OFF_A + i] = cp.pool[pi][4 + i];
+      for (int i = 0; i < P; ++i) o[L::OFF_P + i] = cp.pool[pi][4 + A + i];
+      ent.ref[k] = SWR_CLIP_REF | id;
+    }
+  }
+  ent.n = (uint16_t)cp.npoly;
+  ent.keep = (uint16_t)keep;
+  ent.swap = (uint16_t)swap;
+  g.clip_table[slot] = ent;
+  g.clip_slot[gp] = slot;
+  g.tri_flags[gp] = 4;
+  in_kept = keep & 1u;
+  ex_kept = __popc(keep >> 1);
+}
+
+template <int A, int P>
+__global__ void __launch_bounds__(256) k_assemble_count(AssembleArgs g) {
+  __shared__ uint32_t tmp[32];
+  const uint32_t b = blockIdx.x;
+  const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
+  const SwrDrawDesc& D = g.draws[d];
+  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
+  uint32_t in_sum = 0, ex_sum = 0;
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t p = p0 + threadIdx.x * 4 + j;
+    if (p < D.nprims && p < p0 + SWR_BATCH_PRIMS) {
+      uint32_t ik, ek;
+      assemble_one<A, P>(g, D, d, p, ik, ek);
+      in_sum += ik;
+      ex_sum += ek;
+    }
+  }
+  const uint32_t packed_in = in_sum, packed_ex = ex_sum;
+  uint32_t tin, tex;
+  swr_block_exscan(packed_in, tmp, &tin);
+  swr_block_exscan(packed_ex, tmp, &tex);
+  if (threadIdx.x == 0) g.batch_counts[b] = make_uint2(tin, tex);
+}
+
+// Exclusive scan of per-batch totals -> batch bases; primitive total into the status word.
+static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts, uint32_t nbatches, uint32_t* base,
+                                                     uint32_t* status, uint32_t cap_prims) {
+  __shared__ uint32_t tmp[32];
+  uint32_t run = 0;
+  for (uint32_t b0 = 0; b0 < nbatches; b0 += 1024) {
+    const uint32_t b = b0 + threadIdx.x;
+    const uint32_t v = b < nbatches ? counts[b].x + counts[b].y : 0u;
+    uint32_t tot;
+    const uint32_t ex = swr_block_exscan(v, tmp, &tot);
+    if (b < nbatches) base[b] = run + ex;
+    run += tot;
+  }
+  if (threadIdx.x == 0) {
+    status[SWR_ST_PRIMS] = run;
+    if (run > cap_prims) atomicOr(&status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
+  }
+}
+
+template <int A, int P>
+__global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
+  __shared__ uint32_t tmp[32];
+  if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  const uint32_t b = blockIdx.x;
+  const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
+  const SwrDrawDesc& D = g.draws[d];
+  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
+  uint32_t fl[4], slot[4], in_sum = 0, ex_sum = 0;
+  uint16_t keep[4];
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t p = p0 + threadIdx.x * 4 + j;
+    fl[j] = 0;
+    keep[j] = 0;
+    slot[j] = 0xffffffffu;
+    if (p < D.nprims && p < p0 + SWR_BATCH_PRIMS) {
+      fl[j] = g.tri_flags[D.pbase + p];
+      if (fl[j] & 4) {
+        slot[j] = g.clip_slot[D.pbase + p];
+        if (slot[j] != 0xffffffffu) keep[j] = g.clip_table[slot[j]].keep;
+      } else {
+        keep[j] = fl[j] & 1;
+      }
+      in_sum += keep[j] & 1;
+      ex_sum += __popc(keep[j] >> 1);
+    }
+  }
+  uint32_t tin, tex;
+  uint32_t rin = swr_block_exscan(in_sum, tmp, &tin);
+  uint32_t rex = swr_block_exscan(ex_sum, tmp, &tex);
+  const uint32_t base = g.batch_base[b];
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t p = p0 + threadIdx.x * 4 + j;
+    if (!keep[j]) continue;
+    if (!(fl[j] & 4)) {
+      uint32_t r0 = D.vbase + D.indices[3 * p], r1 = D.vbase + D.indices[3 * p + 1],
+               r2 = D.vbase + D.indices[3 * p + 2];
+      if (fl[j] & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
+      g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
+      rin++;
+    } else {
+      const SwrClipEntry e = g.clip_table[slot[j]];
+      for (int k = 0; k + 2 < e.n; ++k) {
+        if (!((e.keep >> k) & 1)) continue;
+        uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
+        if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
+        if (k == 0) {
+          g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
+          rin++;
+        } else {
+          g.tris[base + tin + rex] = make_uint4(r0, r1, r2, (uint32_t)d);
+          rex++;
+        }
+      }
+    }
+  }
+}
+
+// Direct Rasterizer path: triangles whose first index is -1 are skipped
+// (Rasterizer::drawTriangleList, Rasterizer.h:134-141); others keep their order.
+static __global__ void k_direct_flags(const int32_t* __restrict__ idx, uint32_t nprims, int per,
+                               uint32_t* __restrict__ keep) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < nprims; p += gridDim.x * blockDim.x)
+    keep[p] = idx[(size_t)per * p] != -1 ? 1u : 0u;
+}
+
+static __global__ void k_direct_emit(const int32_t* __restrict__ idx, uint32_t nprims, int per, uint32_t nverts,
+                              const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos,
+                              uint4* __restrict__ tris, uint32_t* status) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < nprims; p += gridDim.x * blockDim.x) {
+    if (!keep[p]) continue;
+    uint32_t r[3] = {0, 0, 0};
+    for (int k = 0; k < per; ++k) {
+      const int32_t i = idx[(size_t)per * p + k];
+      if (i < 0 || (uint32_t)i >= nverts) {
+        atomicOr(&status[SWR_ST_FLAGS], SWR_F_BAD_INDEX);
+        r[k] = 0;
+      } else {
+        r[k] = (uint32_t)i;
+      }
+    }
+    tris[pos[p]] = make_uint4(r[0], r[1], r[2], 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Triangle setup.
+
+// Setup record layout for pixel shader PS (32-bit words).
+template <class PS>
+struct Rec {
+  enum {
+    NA = PS::AVarCount,
+    NP = PS::PVarCount,
+    IZ = PS::InterpolateZ ? 1 : 0,
+    IW = (PS::InterpolateW || PS::PVarCount > 0) ? 1 : 0,
+    NEQ = IZ + IW + NA + NP,
+    EQ0 = 18,
+    R = ((EQ0 + 3 * NEQ + 3) / 4) * 4,
+    EQ_Z = 0,
+    EQ_W = IZ,
+    EQ_A = IZ + IW,
+    EQ_P = IZ + IW + NA
+  };
+  // word 0 flags: bit0 drawable, bit1 block mode, bits2-4 tie of e0..e2, bit5 bottom half,
+  //               bit6 top half
+  // word 1 draw id; words 2-5 pixel bbox x0, y0, x1, y1 (inclusive, clamped to target)
+  // block: words 6-14 e0.a e0.b e0.c e1.a e1.b e1.c e2.a e2.b e2.c
+  // span:  words 6-11 bottom half yb0 yb1 t.x t.y is1 is2; 12-17 top half yt_hi yt_lo b.x b.y is1 is2
+  // words 18.. (a, b, c) per interpolated equation: z, invw, avar[NA], pvar[NP]
+};
+
+struct Edge {
+  float a, b, c;
+  bool tie;
+};
+
+__device__ __forceinline__ Edge make_edge(float x0, float y0, float x1, float y1) {
+  // EdgeEquation::init (EdgeEquation.h:37-43)
+  Edge e;
+  e.a = swr_sub(y0, y1);
+  e.b = swr_sub(x1, x0);
+  e.c = swr_div(-swr_add(swr_mul(e.a, swr_add(x0, x1)), swr_mul(e.b, swr_add(y0, y1))), 2.0f);
+  e.tie = e.a != 0.0f ? e.a > 0.0f : e.b > 0.0f;
+  return e;
+}
+
+__device__ __forceinline__ bool edge_test(float v, bool tie) { return v > 0.0f || (v == 0.0f && tie); }
+
+__device__ __forceinline__ void param_eq(float p0, float p1, float p2, const Edge& e0, const Edge& e1,
+                                         const Edge& e2, float f, float* o) {
+  // ParameterEquation::init (ParameterEquation.h:36-48)
+  o[0] = swr_mul(f, swr_add(swr_add(swr_mul(p0, e0.a), swr_mul(p1, e1.a)), swr_mul(p2, e2.a)));
+  o[1] = swr_mul(f, swr_add(swr_add(swr_mul(p0, e0.b), swr_mul(p1, e1.b)), swr_mul(p2, e2.b)));
+  o[2] = swr_mul(f, swr_add(swr_add(swr_mul(p0, e0.c), swr_mul(p1, e1.c)), swr_mul(p2, e2.c)));
+}
+
+struct SetupArgs {
+  const uint4* tris;
+  const uint32_t* status;  // SWR_ST_PRIMS = primitive count
+  uint32_t cap_prims;
+  const float* ptv;
+  const float* clipv;
+  int S, off_a, off_p, vs_a, vs_p;
+  const SwrDrawDesc* draws;
+  const SwrTargetDesc* targets;
+  float* recs;
+  uint32_t* tile_count;
+  int tile;  // tile edge in pixels
+};
+
+struct SpanHalf {
+  float ox, oy, is1, is2;
+  int y0, y1;  // bottom: rows [y0, y1); top: rows (y1, y0]
+};
+
+// x extent (xl of the first pixel, xr exclusive) of row y of a span half.
+__device__ __forceinline__ void span_row(const SpanHalf& h, int y, int minx, int maxx, int& xl, int& xr) {
+  const float dy = swr_add(swr_sub((float)y, h.oy), 0.5f);
+  const float c1 = swr_add(swr_add(h.ox, swr_mul(h.is1, dy)), 0.5f);
+  const float c2 = swr_add(swr_add(h.ox, swr_mul(h.is2, dy)), 0.5f);
+  xl = swr_maxi(minx, swr_trunc_int(c1));
+  xr = swr_mini(maxx, swr_trunc_int(c2));
+}
+
+template <class PS>
+__global__ void __launch_bounds__(256) k_setup(SetupArgs g) {
+  typedef Rec<PS> RL;
+  if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  uint32_t np = g.status[SWR_ST_PRIMS];
+  if (np > g.cap_prims) np = g.cap_prims;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const uint4 t = g.tris[p];
+    const SwrDrawDesc& D = g.draws[t.w];
+    const SwrTargetDesc& T = g.targets[D.target];
+    const uint32_t rr[3] = {t.x, t.y, t.z};
+    float x[3], y[3], z[3], w[3];
+    const float* vp[3];
+    for (int k = 0; k < 3; ++k) {
+      vp[k] = (rr[k] & SWR_CLIP_REF) ? g.clipv + (size_t)(rr[k] & ~SWR_CLIP_REF) * g.S : g.ptv + (size_t)rr[k] * g.S;
+      x[k] = vp[k][4]; y[k] = vp[k][5]; z[k] = vp[k][6]; w[k] = vp[k][3];
+    }
+    float* rec = g.recs + (size_t)p * RL::R;
+    uint32_t tiles = 0;
+    // TriangleEquations: e0 = (v1, v2), e1 = (v2, v0), e2 = (v0, v1)
+    const Edge e0 = make_edge(x[1], y[1], x[2], y[2]);
+    const Edge e1 = make_edge(x[2], y[2], x[0], y[0]);
+    const Edge e2 = make_edge(x[0], y[0], x[1], y[1]);
+    const float area2 = swr_add(swr_add(e0.c, e1.c), e2.c);
+    int flags = 0;
+    int bx0 = 0, by0 = 0, bx1 = -1, by1 = -1;
+    if (!(area2 <= 0.0f)) {
+      flags = 1 | (e0.tie ? 4 : 0) | (e1.tie ? 8 : 0) | (e2.tie ? 16 : 0);
+      const float factor = swr_div(1.0f, area2);
+      float* eq = rec + RL::EQ0;
+      if (RL::IZ) param_eq(z[0], z[1], z[2], e0, e1, e2, factor, eq + 3 * RL::EQ_Z);
+      const float iw0 = swr_div(1.0f, w[0]), iw1 = swr_div(1.0f, w[1]), iw2 = swr_div(1.0f, w[2]);
+      if (RL::IW) param_eq(iw0, iw1, iw2, e0, e1, e2, factor, eq + 3 * RL::EQ_W);
+      for (int i = 0; i < RL::NA; ++i) {
+        float a[3];
+        for (int k = 0; k < 3; ++k) a[k] = i < g.vs_a ? vp[k][g.off_a + i] : 0.0f;
+        param_eq(a[0], a[1], a[2], e0, e1, e2, factor, eq + 3 * (RL::EQ_A + i));
+      }
+      for (int i = 0; i < RL::NP; ++i) {
+        float a[3];
+        for (int k = 0; k < 3; ++k) a[k] = i < g.vs_p ? vp[k][g.off_p + i] : 0.0f;
+        param_eq(swr_mul(a[0], iw0), swr_mul(a[1], iw1), swr_mul(a[2], iw2), e0, e1, e2, factor,
+                 eq + 3 * (RL::EQ_P + i));
+      }
+      // Raster mode (Rasterizer.h:414-446); Adaptive compares the float ratio as double.
+      bool block = D.raster_mode == 1;
+      if (D.raster_mode == 2) {
+        const float fx0 = swr_minf(swr_minf(x[0], x[1]), x[2]), fx1 = swr_maxf(swr_maxf(x[0], x[1]), x[2]);
+        const float fy0 = swr_minf(swr_minf(y[0], y[1]), y[2]), fy1 = swr_maxf(swr_maxf(y[0], y[1]), y[2]);
+        const float orient = swr_div(swr_sub(fx1, fx0), swr_sub(fy1, fy0));
+        block = (double)orient > 0.4 && (double)orient < 1.6;
+      }
+      if (block) {
+        flags |= 2;
+        // Rasterizer.h:235-255
+        int mnx = swr_trunc_int(swr_minf(swr_minf(x[0], x[1]), x[2]));
+        int mxx = swr_trunc_int(swr_maxf(swr_maxf(x[0], x[1]), x[2]));
+        int mny = swr_trunc_int(swr_minf(swr_minf(y[0], y[1]), y[2]));
+        int mxy = swr_trunc_int(swr_maxf(swr_maxf(y[0], y[1]), y[2]));
+        mnx = swr_maxi(mnx, D.sc_minx);
+        mxx = swr_mini(mxx, D.sc_maxx);
+        mny = swr_maxi(mny, D.sc_miny);
+        mxy = swr_mini(mxy, D.sc_maxy);
+        mnx &= ~(SWR_BLOCK - 1);
+        mxx &= ~(SWR_BLOCK - 1);
+        mny &= ~(SWR_BLOCK - 1);
+        mxy &= ~(SWR_BLOCK - 1);
+        const int sx = (mxx - mnx) / SWR_BLOCK + 1, sy = (mxy - mny) / SWR_BLOCK + 1;
+        // Blocks visited by i in [0, sx*sy): (mnx + (i % sx) * 8, mny + (i / sx) * 8).
+        if (sx > 0 && sy > 0) {
+          bx0 = mnx; bx1 = mnx + SWR_BLOCK * (sx - 1) + SWR_BLOCK - 1;
+          by0 = mny; by1 = mny + SWR_BLOCK * (sy - 1) + SWR_BLOCK - 1;
+        } else if (sx < 0 && sy < 0) {
+          bx0 = mnx; bx1 = mnx + SWR_BLOCK * (-sx - 1) + SWR_BLOCK - 1;
+          by0 = mny - SWR_BLOCK * (-sy - 1); by1 = mny + SWR_BLOCK - 1;
+        }
+        rec[6] = e0.a; rec[7] = e0.b; rec[8] = e0.c;
+        rec[9] = e1.a; rec[10] = e1.b; rec[11] = e1.c;
+        rec[12] = e2.a; rec[13] = e2.b; rec[14] = e2.c;
+      } else {
+        // Rasterizer.h:318-357
+        int it = 0, im = 1, ib = 2;
+        if (y[it] > y[im]) { const int q = it; it = im; im = q; }
+        if (y[im] > y[ib]) { const int q = im; im = ib; ib = q; }
+        if (y[it] > y[im]) { const int q = it; it = im; im = q; }
+        const float dy = swr_sub(y[ib], y[it]);
+        const float iy = swr_sub(y[im], y[it]);
+        SpanHalf bot, top;
+        bool has_bot = false, has_top = false;
+        float lx, ly, rx, ry;
+        if (y[im] == y[it]) {
+          lx = x[im]; ly = y[im]; rx = x[it]; ry = y[it];
+          if (lx > rx) { float q = lx; lx = rx; rx = q; q = ly; ly = ry; ry = q; }
+          has_top = true;
+        } else if (y[im] == y[ib]) {
+          lx = x[im]; ly = y[im]; rx = x[ib]; ry = y[ib];
+          if (lx > rx) { float q = lx; lx = rx; rx = q; q = ly; ly = ry; ry = q; }
+          has_bot = true;
+        } else {
+          const float v4x = swr_add(x[it], swr_mul(swr_div(swr_sub(x[ib], x[it]), dy), iy));
+          lx = x[im]; ly = y[im]; rx = v4x; ry = y[im];
+          if (lx > rx) { float q = lx; lx = rx; rx = q; q = ly; ly = ry; ry = q; }
+          has_bot = has_top = true;
+        }
+        if (has_bot) {  // drawBottomFlatTriangle(t, l, r) (Rasterizer.h:361-385)
+          bot.ox = x[it]; bot.oy = y[it];
+          bot.is1 = swr_div(swr_sub(lx, x[it]), swr_sub(ly, y[it]));
+          bot.is2 = swr_div(swr_sub(rx, x[it]), swr_sub(ry, y[it]));
+          bot.y0 = swr_trunc_int(swr_add(y[it], 0.5f));
+          bot.y1 = swr_trunc_int(swr_add(ly, 0.5f));
+        } else {
+          bot.ox = bot.oy = bot.is1 = bot.is2 = 0.0f;
+          bot.y0 = bot.y1 = 0;
+        }
+        if (has_top) {  // drawTopFlatTriangle(l, r, b) (Rasterizer.h:388-411)
+          top.ox = x[ib]; top.oy = y[ib];
+          top.is1 = swr_div(swr_sub(x[ib], lx), swr_sub(y[ib], ly));
+          top.is2 = swr_div(swr_sub(x[ib], rx), swr_sub(y[ib], ry));
+          top.y0 = swr_trunc_int(swr_sub(y[ib], 0.5f));
+          top.y1 = swr_trunc_int(swr_sub(ly, 0.5f));
+        } else {
+          top.ox = top.oy = top.is1 = top.is2 = 0.0f;
+          top.y0 = top.y1 = 0;
+        }
+        if (has_bot) flags |= 32;
+        if (has_top) flags |= 64;
+        rec[6] = __int_as_float(bot.y0); rec[7] = __int_as_float(bot.y1);
+        rec[8] = bot.ox; rec[9] = bot.oy; rec[10] = bot.is1; rec[11] = bot.is2;
+        rec[12] = __int_as_float(top.y0); rec[13] = __int_as_float(top.y1);
+        rec[14] = top.ox; rec[15] = top.oy; rec[16] = top.is1; rec[17] = top.is2;
+        // Conservative pixel box: rows inside the target, x from the end rows of each
+        // half (the span edges are linear in y up to rounding, hence the 2 px margin).
+        int rx0 = 0x7fffffff, rx1 = -0x7fffffff, ry0 = 0x7fffffff, ry1 = -0x7fffffff;
+        for (int hh = 0; hh < 2; ++hh) {
+          const SpanHalf& h = hh ? top : bot;
+          if (!(hh ? has_top : has_bot)) continue;
+          int lo = hh ? h.y1 + 1 : h.y0, hi = hh ? h.y0 : h.y1 - 1;
+          lo = swr_maxi(lo, 0);
+          hi = swr_mini(hi, T.height - 1);
+          if (lo > hi) continue;
+          ry0 = swr_mini(ry0, lo);
+          ry1 = swr_maxi(ry1, hi);
+          for (int e = 0; e < 2; ++e) {
+            int xl, xr;
+            span_row(h, e ? hi : lo, D.sc_minx, D.sc_maxx, xl, xr);
+            rx0 = swr_mini(rx0, xl);
+            rx1 = swr_maxi(rx1, xr - 1);
+          }
+        }
+        if (ry0 <= ry1) {
+          bx0 = swr_maxi(rx0 - 2, D.sc_minx);
+          bx1 = swr_mini(rx1 + 2, D.sc_maxx - 1);
+          by0 = ry0;
+          by1 = ry1;
+        }
+      }
+      bx0 = swr_maxi(bx0, 0);
+      by0 = swr_maxi(by0, 0);
+      bx1 = swr_mini(bx1, T.width - 1);
+      by1 = swr_mini(by1, T.height - 1);
+      if (bx0 <= bx1 && by0 <= by1) {
+        const int tx0 = bx0 / g.tile, tx1 = bx1 / g.tile, ty0 = by0 / g.tile, ty1 = by1 / g.tile;
+        tiles = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+      } else {
+        flags = 0;
+      }
+    }
+    rec[0] = __int_as_float(flags);
+    rec[1] = __int_as_float((int)t.w);
+    rec[2] = __int_as_float(bx0); rec[3] = __int_as_float(by0);
+    rec[4] = __int_as_float(bx1); rec[5] = __int_as_float(by1);
+    g.tile_count[p] = flags ? tiles : 0u;
+  }
+}
+
+// (tile, primitive) pairs in primitive order.
+template <class PS>
+__global__ void __launch_bounds__(256) k_emit_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs,
+                                                    const uint32_t* tile_count, const uint32_t* pair_off,
+                                                    const uint32_t* npairs, uint32_t cap_pairs,
+                                                    const SwrDrawDesc* draws, const SwrTargetDesc* targets,
+                                                    int tile, uint32_t* keys, uint32_t* vals,
+                                                    uint32_t* status_w) {
+  typedef Rec<PS> RL;
+  if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  if (*npairs > cap_pairs) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicOr(&status_w[SWR_ST_FLAGS], SWR_F_PAIR_OVERFLOW);
+      status_w[SWR_ST_PAIRS] = *npairs;
+    }
+    return;
+  }
+  uint32_t np = status[SWR_ST_PRIMS];
+  if (np > cap_prims) np = cap_prims;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    if (!tile_count[p]) continue;
+    const float* rec = recs + (size_t)p * RL::R;
+    const int d = __float_as_int(rec[1]);
+    const SwrTargetDesc& T = targets[draws[d].target];
+    const int tx0 = __float_as_int(rec[2]) / tile, ty0 = __float_as_int(rec[3]) / tile;
+    const int tx1 = __float_as_int(rec[4]) / tile, ty1 = __float_as_int(rec[5]) / tile;
+    uint32_t o = pair_off[p];
+    for (int ty = ty0; ty <= ty1; ++ty)
+      for (int tx = tx0; tx <= tx1; ++tx) {
+        keys[o] = T.tile_base + (uint32_t)(ty * T.tiles_x + tx);
+        vals[o] = p;
+        o++;
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Tile rasterization.
+
+template <class PS>
+struct GpuPixel {  // PixelData (PixelData.h:35-146) as seen by drawPixel
+  int x, y;
+  float z, w, invw;
+  float avar[PS::AVarCount > 0 ? PS::AVarCount : 1];
+  float pvar[PS::PVarCount > 0 ? PS::PVarCount : 1];
+};
+
+struct RasterArgs {
+  const uint32_t* status;
+  const uint32_t* tile_start;  // per global tile, plus one
+  const uint32_t* bin;         // primitive ids sorted by tile
+  const float* recs;
+  const SwrDrawDesc* draws;
+  const SwrTargetDesc* targets;
+  const uint32_t* target_tile_base;  // per target, for the tile -> target lookup
+  int ntargets;
+  uint32_t* status_w;
+};
+
+template <class PS, int TILE, int CH>
+__global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
+  typedef Rec<PS> RL;
+  constexpr int PPT = TILE * TILE / 256;  // pixels per thread
+  __shared__ float srec[CH * RL::R];
+  __shared__ uint32_t sids[CH];
+  __shared__ uint32_t sfr[32];
+  if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t b = g.tile_start[tile], e = g.tile_start[tile + 1];
+  if (b == e) return;
+  const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
+  const SwrTargetDesc& T = g.targets[ti];
+  const SwrUniforms& U = g.draws[T.first_draw].u;
+  const uint32_t lt = tile - T.tile_base;
+  const int ox = (int)(lt % (uint32_t)T.tiles_x) * TILE, oy = (int)(lt / (uint32_t)T.tiles_x) * TILE;
+  // Thread -> pixels: each warp covers an 8 x 4 half block; sub-tiles of 16 x 16 repeat.
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int px[PPT], py[PPT];
+  bool in[PPT];
+  typename PS::State st[PPT];
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) {
+    const int sub = q;  // 16x16 sub-tile index
+    const int sxo = (sub % (TILE / 16)) * 16, syo = (sub / (TILE / 16)) * 16;
+    const int blk = warp >> 1;
+    px[q] = ox + sxo + (blk & 1) * 8 + (lane & 7);
+    py[q] = oy + syo + (blk >> 1) * 8 + (warp & 1) * 4 + (lane >> 3);
+    in[q] = px[q] < T.width && py[q] < T.height;
+    if (in[q]) PS::load(st[q], px[q], py[q], U);
+  }
+  uint32_t frags = 0;
+  for (uint32_t c0 = b; c0 < e; c0 += CH) {
+    const int n = (int)min((uint32_t)CH, e - c0);
+    __syncthreads();
+    if (threadIdx.x < n) sids[threadIdx.x] = g.bin[c0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n * RL::R; i += 256) {
+      const int k = i / RL::R, w = i - k * RL::R;
+      srec[i] = g.recs[(size_t)sids[k] * RL::R + w];
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+      const float* r = srec + k * RL::R;
+      const int flags = __float_as_int(r[0]);
+      const int x0 = __float_as_int(r[2]), y0 = __float_as_int(r[3]);
+      const int x1 = __float_as_int(r[4]), y1 = __float_as_int(r[5]);
+      const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+      const float* eq = r + RL::EQ0;
+#pragma unroll
+      for (int q = 0; q < PPT; ++q) {
+        if (!in[q] || px[q] < x0 || px[q] > x1 || py[q] < y0 || py[q] > y1) continue;
+        float fx, fy;
+        int ka, kb;  // steps along a (x) and b (y) from the evaluation point
+        if (flags & 2) {
+          const int bx = px[q] & ~(SWR_BLOCK - 1), by = py[q] & ~(SWR_BLOCK - 1);
+          fx = swr_add((float)bx, 0.5f);
+          fy = swr_add((float)by, 0.5f);
+          bool t00[3], t01[3], t10[3], t11[3];
+          float ev[3];
+          const float s = (float)(SWR_BLOCK - 1);
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float ea = r[6 + 3 * j], eb = r[7 + 3 * j], ec = r[8 + 3 * j];
+            const bool tie = (flags >> (2 + j)) & 1;
+            ev[j] = swr_eval(ea, eb, ec, fx, fy);
+            const float v01 = swr_add(ev[j], swr_mul(eb, s));
+            const float v10 = swr_add(ev[j], swr_mul(ea, s));
+            const float v11 = swr_add(v01, swr_mul(ea, s));
+            t00[j] = edge_test(ev[j], tie);
+            t01[j] = edge_test(v01, tie);
+            t10[j] = edge_test(v10, tie);
+            t11[j] = edge_test(v11, tie);
+          }
+          const int inside = (t00[0] && t00[1] && t00[2]) + (t01[0] && t01[1] && t01[2]) +
+                             (t10[0] && t10[1] && t10[2]) + (t11[0] && t11[1] && t11[2]);
+          kb = py[q] - by;
+          ka = px[q] - bx;
+          bool test = true;
+          if (inside == 0) {
+            const bool s00 = (t00[0] == t00[1]) == t00[2], s01 = (t01[0] == t01[1]) == t01[2];
+            const bool s10 = (t10[0] == t10[1]) == t10[2], s11 = (t11[0] == t11[1]) == t11[2];
+            if (s00 && s01 && s10 && s11) continue;
+          } else if (inside == 4) {
+            test = false;
+          }
+          if (test) {
+            bool ok = true;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const float v = swr_fold(swr_fold(ev[j], r[7 + 3 * j], kb), r[6 + 3 * j], ka);
+              ok = ok && edge_test(v, (flags >> (2 + j)) & 1);
+            }
+            if (!ok) continue;
+          }
+        } else {
+          int xl, xr;
+          SpanHalf h;
+          const int y = py[q];
+          if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
+            h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
+          } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
+            h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
+          } else {
+            continue;
+          }
+          span_row(h, y, D.sc_minx, D.sc_maxx, xl, xr);
+          if (px[q] < xl || px[q] >= xr) continue;
+          fx = swr_add((float)xl, 0.5f);
+          fy = swr_add((float)y, 0.5f);
+          ka = px[q] - xl;
+          kb = 0;
+        }
+        GpuPixel<PS> pd;
+        pd.x = px[q];
+        pd.y = py[q];
+        if (RL::IZ) {
+          const float* q3 = eq + 3 * RL::EQ_Z;
+          pd.z = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+        }
+        if (RL::IW) {
+          const float* q3 = eq + 3 * RL::EQ_W;
+          pd.invw = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          pd.w = swr_div(1.0f, pd.invw);
+        }
+#pragma unroll
+        for (int i = 0; i < RL::NA; ++i) {
+          const float* q3 = eq + 3 * (RL::EQ_A + i);
+          pd.avar[i] = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+        }
+#pragma unroll
+        for (int i = 0; i < RL::NP; ++i) {
+          const float* q3 = eq + 3 * (RL::EQ_P + i);
+          const float pt = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          pd.pvar[i] = swr_mul(pt, pd.w);
+        }
+        PS::drawPixel(pd, (int)sids[k], st[q], D.u);
+        frags++;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < PPT; ++q)
+    if (in[q]) PS::store(st[q], px[q], py[q], U);
+  // fragment statistics
+  uint32_t tot;
+  swr_block_exscan(frags, sfr, &tot);
+  if (threadIdx.x == 0 && tot) {
+    const unsigned long long old = atomicAdd((unsigned long long*)&g.status_w[SWR_ST_SHADED_LO], (unsigned long long)tot);
+    (void)old;
+  }
+}
+
+}  // namespace swr

@@ -1,0 +1,71 @@
+"""GPU parity: the CUDA pipeline against the CPU oracle (bit-exact).
+
+Every buffer the pixel shaders write is compared bit for bit: colour, depth, per-pixel
+drawPixel count (covered-pixel set and fragment count) and the id of the primitive that
+won the depth test.  Shaded colours are computed with the same IEEE operations on both
+sides, so the stated colour tolerance (max abs error <= 2^-20 on FP32 outputs) is met with
+zero error; the comparison is exact.
+"""
+import numpy as np
+import pytest
+
+from softwarerenderer_gb300 import scenes
+from softwarerenderer_gb300.abi import DrawMode, RasterMode
+
+from .parity import describe, diff, gpu_render, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+TRI_SEEDS = list(range(0, 160))
+
+
+def _check(port, sc, tile=16):
+    ref, rst = oracle_render(port, sc)
+    got, gst = gpu_render(sc, tile=tile)
+    bad = diff(ref, got)
+    msgs = [describe(ref, got, k) for k in bad]
+    assert not bad, f"{sc.name} {sc.draw_mode.name} {sc.raster.name}: " + "; ".join(msgs)
+    assert gst["fragments"] == rst["fragments"], (sc.name, gst, rst)
+    return rst
+
+
+@pytest.mark.parametrize("seed", TRI_SEEDS)
+def test_random_triangles(gpu_lib, port, seed):
+    sc = scenes.random_scene(seed, draw_mode=DrawMode.Triangle)
+    _check(port, sc)
+
+
+@pytest.mark.parametrize("seed", range(0, 24))
+def test_random_triangles_tile32(gpu_lib, port, seed):
+    sc = scenes.random_scene(1000 + seed, draw_mode=DrawMode.Triangle)
+    _check(port, sc, tile=32)
+
+
+@pytest.mark.parametrize("frame", [0, 1, 17, 42, 99])
+def test_cube_frames(gpu_lib, port, frame):
+    st = _check(port, scenes.cube_scene(frame))
+    assert st["fragments"] > 0
+
+
+@pytest.mark.parametrize("pose", [0, 3, 8, 13, 25, 31])
+def test_sphere7_poses(gpu_lib, port, pose):
+    st = _check(port, scenes.sphere_scene(pose))
+    assert st["fragments"] > 0
+
+
+@pytest.mark.parametrize("mode", [RasterMode.Span, RasterMode.Block, RasterMode.Adaptive])
+def test_sphere5_all_modes(gpu_lib, port, mode):
+    _check(port, scenes.sphere_scene(4, level=5, width=640, height=360, raster=mode))
+
+
+def test_soup_adaptive_64k(gpu_lib, port):
+    st = _check(port, scenes.soup_scene(1 << 16))
+    assert st["fragments"] > 1_000_000
+
+
+def test_batch_boundary_clip_fans(gpu_lib, port):
+    """Clip fans are appended after the whole 1024-primitive batch (VertexProcessor.cpp:254-260)."""
+    # 3000 triangles crossing the near plane straddle two batch boundaries.
+    for seed in (7, 8):
+        sc = scenes.random_scene(seed, direct=False, draw_mode=DrawMode.Triangle, n_prims=3000)
+        _check(port, sc)
