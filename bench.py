@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 rasterization pipeline on the dense-mesh workload.
+
+Workload: icosphere subdivision 7 (163,842 vertices / 327,680 triangles; position+normal
+24 B and uv 8 B per vertex, uint32 indices), 1920x1080 target, RasterMode Block, CullMode
+CW, Lambert + procedural checker pixel shader with FP32 depth test, 32 seeded camera poses
+of which 3 put the near plane through the mesh.  One step = one frame: clear colour and
+depth, set the pose, VertexProcessor::drawElements over all 983,040 indices.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+`value` is shaded fragments per second over the K timed frames (device time from CUDA
+events around each frame, L2 flushed with a 256 MiB write before every frame); Mtris/s is
+reported beside it.  `e2e` repeats the measurement through the public API with the
+step's vertex/index buffers copied host->device from pinned memory and the colour buffer
+copied back inside the timed region.  `--impl reference` times the reference algorithm on
+the host cores instead (the CPU oracle port; the reference's own sources are not on the
+benchmark machine).  With N > 1 (torchrun) every rank renders the same frames on its own
+GPU: replicas, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gfrags/s & Mtris/s at 1080p on 1 GB300; batched views/s, fwd+bwd/s vs plain"
+WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + uv 8 B, uint32 "
+            "indices), 1920x1080, RasterMode Block, CullMode CW, Lambert + checker, FP32 depth "
+            "test, 32 seeded poses (3 near-plane clipped), 1 frame per step")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def frame_bytes(n_idx, vertex_bytes, pixels, frags, passes, texel_bytes=0):
+    """Algorithmic bytes of one frame (index + vertex streams read once, colour+depth
+    clear/store per target pixel, depth read per fragment, depth+RGBA8 write per pass)."""
+    return 4 * n_idx + vertex_bytes + 8 * pixels + 4 * frags + 8 * passes + texel_bytes * frags
+
+
+def cpu_baseline(min_seconds=10.0, max_frames=32):
+    """The reference algorithm (CPU oracle port) on host cores, best of 1 thread and all."""
+    from oracle import oracle
+    from softwarerenderer_gb300 import scenes
+    port = oracle.load("port")
+    ncores = os.cpu_count() or 1
+    results = {}
+    for threads in sorted({1, ncores}):
+        frags, t_tot, n = 0, 0.0, 0
+        while n < max_frames and (t_tot < min_seconds / 2 or n < 2):
+            sc = scenes.sphere_scene(n % 32)
+            tg = scenes.Target(sc, aux=False)
+            t0 = time.perf_counter()
+            st = port.draw(sc, tg, threads=threads)
+            t_tot += time.perf_counter() - t0
+            frags += st["fragments"]
+            n += 1
+        results[threads] = (frags / t_tot / 1e9, n, t_tot, 327680 * n / t_tot / 1e6)
+    best = max(results, key=lambda k: results[k][0])
+    v, n, t, mtris = results[best]
+    return {"value": v, "unit": "Gfrags/s", "cores": best, "kind": "port",
+            "sample": f"{n} of the 32 poses, {t:.1f} s of CPU time at {best} thread(s) "
+                      f"(best of 1 and {ncores} threads; OpenMP as in the reference)",
+            "mtris_per_s": mtris,
+            "by_threads": {str(k): round(r[0], 4) for k, r in results.items()}}
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference algorithm (CPU oracle port, OpenMP where the reference
+    has it) with every host thread, W warm-up and K timed frames of the same workload."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    from softwarerenderer_gb300 import scenes
+    port = oracle.load("port")
+    ncores = os.cpu_count() or 1
+    for k in range(args.warmup):
+        sc = scenes.sphere_scene(k % 32)
+        port.draw(sc, scenes.Target(sc, aux=False), threads=ncores)
+    frags, t_tot = 0, 0.0
+    for k in range(args.steps):
+        sc = scenes.sphere_scene(k % 32)
+        tg = scenes.Target(sc, aux=False)
+        t0 = time.perf_counter()
+        st = port.draw(sc, tg, threads=ncores)
+        t_tot += time.perf_counter() - t0
+        frags += st["fragments"]
+    value = frags / t_tot / 1e9
+    cb = {"value": value, "unit": "Gfrags/s", "cores": ncores, "kind": "port",
+          "sample": f"{args.steps} frames (poses 0..{min(args.steps, 32) - 1}), {t_tot:.1f} s"}
+    line = {"metric": METRIC, "value": value, "unit": "Gfrags/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_tot / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded icosphere and poses)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "engine": "CPU oracle port of VertexProcessor+Rasterizer",
+                       "threads": ncores},
+            "mtris_per_s": 327680 * args.steps / t_tot / 1e6,
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "Gfrags/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--tile", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    assert args.warmup >= 3, "at least 3 warm-up steps"
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(local)
+
+    from softwarerenderer_gb300 import build, scenes
+    if not os.path.exists(build.LIB):
+        build.build()
+    from softwarerenderer_gb300.abi import make_uniforms
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+
+    sc = scenes.sphere_scene(0)
+    poses = [scenes.sphere_scene(p).mvp for p in range(scenes.SPHERE_POSES)]
+    ds = DeviceScene(sc, tile=args.tile)
+    tg = DeviceTarget(sc, aux=False)
+    ctx = ds.rast.ctx
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")  # 256 MiB > L2
+    stream = torch.cuda.current_stream()
+    ds.bind(tg)
+
+    def frame(k):
+        tg.clear()
+        ds.rast.setUniforms(ds.uniforms(tg, poses[k % len(poses)]))
+        ds.vp.drawElements(sc.draw_mode, ds.indices.numel(), ds.indices, sync=False)
+
+    # warm-up (also grows the scratch queues to their steady-state size)
+    for k in range(args.warmup):
+        frame(k)
+        rc, _ = ctx.finish()
+        if rc == 3:  # overflow: queues grown, run again
+            frame(k)
+            ctx.finish()
+    ctx.set_profiling(True)
+    ctx.stage_times()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(k)
+            starts[k].record(stream)
+            frame(k)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    rc, st = ctx.finish()
+    assert rc == 0, f"draw status {rc}"
+    stages = ctx.stage_times()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms_max = ms
+    frags, passes = st["fragments"], st["passes"]
+    if dist:
+        t = torch.tensor([ms, frags], dtype=torch.float64, device="cuda")
+        tm = t.clone()
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms_max = float(tm[0])
+        frags_all = float(t[1])
+    else:
+        frags_all = float(frags)
+    value = frags_all / (ms_max / 1e3) / 1e9
+    mtris = 327680 * args.steps * world / (ms_max / 1e3) / 1e6
+
+    # roofline of the dominant kernel (by stage time)
+    hbm, peak_kind = peaks()
+    dom = max(stages, key=stages.get)
+    n_idx = ds.indices.numel()
+    vbytes = sum(b.numel() for b, _ in ds.attribs)
+    pixels = sc.width * sc.height
+    per_launch = {
+        # fragment terms: depth read per drawPixel call, depth + RGBA8 write per colour write
+        "raster": (4 * frags + 8 * passes) / args.steps,
+        "vertex": vbytes + sc.vertex_count() * 64,   # attribute streams read + post-transform records written
+        "assemble": 4 * n_idx,
+        "setup": 0, "bin": 0,
+    }
+    alg = per_launch.get(dom, 0)
+    t_launch = stages[dom] / args.steps / 1e3
+    achieved = alg / t_launch / 1e9 if t_launch > 0 else 0.0
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get(dom)
+    except Exception:
+        pass
+    roofline = {"bound": "hbm", "kernel": f"k_raster<PsLambert,{args.tile}>" if dom == "raster" else dom,
+                "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 5), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                "launch_ms": round(stages[dom] / args.steps, 4)}
+    fb = frame_bytes(n_idx, vbytes, pixels, frags / args.steps, passes / args.steps)
+    frame_roof = {"bytes_per_frame": fb, "achieved_gbs": round(fb / (ms / args.steps / 1e3) / 1e9, 2),
+                  "frac": round(fb / (ms / args.steps / 1e3) / 1e9 / hbm, 5)}
+
+    # e2e through the public API with host buffers
+    e2e = run_e2e(ds, tg, sc, poses, args, torch)
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cb = cpu_baseline()
+        except Exception as ex:  # pragma: no cover
+            cb = {"error": str(ex)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": "Gfrags/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded icosphere and poses)",
+                "config": {"workload": WORKLOAD, "tile": args.tile, "parallelism": f"replicas x{world}",
+                           "l2": "flushed before every timed frame (256 MiB write)"},
+                "mtris_per_s": round(mtris, 2),
+                "fragments_per_frame": frags / args.steps, "depth_passes_per_frame": passes / args.steps,
+                "stage_ms_per_frame": {k: round(v / args.steps, 4) for k, v in stages.items()},
+                "gpu_launches": int(st["launches"]),
+                "roofline": roofline, "frame_roofline": frame_roof,
+                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(ds, tg, sc, poses, args, torch):
+    """Same frames through VertexProcessor.drawElements with host (pinned) inputs: every step
+    copies the vertex streams and indices host->device and reads the colour buffer back."""
+    hv = [torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory() for a, _ in sc.attribs]
+    hi = torch.from_numpy(np.asarray(sc.indices, np.int32)).pin_memory()
+    hout = torch.empty(tg.color.shape, dtype=tg.color.dtype).pin_memory()
+    stream = torch.cuda.current_stream()
+    h2d = sum(t.numel() for t in hv) + hi.numel() * 4
+    d2h = hout.numel() * 4
+
+    def step(k):
+        for (dbuf, _), hbuf in zip(ds.attribs, hv):
+            dbuf.copy_(hbuf, non_blocking=True)
+        ds.indices.copy_(hi, non_blocking=True)
+        tg.clear()
+        ds.rast.setUniforms(ds.uniforms(tg, poses[k % len(poses)]))
+        ds.vp.drawElements(sc.draw_mode, ds.indices.numel(), ds.indices, sync=False)
+        hout.copy_(tg.color, non_blocking=True)
+
+    for k in range(args.warmup):
+        step(k)
+    ds.rast.ctx.finish()
+    ds.rast.ctx.stage_times()
+    s0 = torch.cuda.Event(enable_timing=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s0.record(stream)
+    for k in range(args.steps):
+        step(k)
+    e0.record(stream)
+    torch.cuda.synchronize()
+    rc, st = ds.rast.ctx.finish()
+    assert rc == 0
+    ms = s0.elapsed_time(e0)
+    return {"value": round(st["fragments"] / (ms / 1e3) / 1e9, 4), "unit": "Gfrags/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": round(ms / args.steps, 4),
+            "mtris_per_s": round(327680 * args.steps / (ms / 1e3) / 1e6, 2)}
+
+
+if __name__ == "__main__":
+    main()

@@ -54,6 +54,8 @@ typedef struct swr_stats {
   uint64_t bin_pairs;   /* (tile, primitive) bin entries of the last draw */
   uint32_t clip_polygons;  /* triangles clipped against the frustum in the last draw */
   uint32_t flags;       /* internal status bits (0 when everything succeeded) */
+  uint64_t launches;    /* kernels this library launched since the last swr_finish */
+  uint64_t passes;      /* colour writes by the pixel shaders (depth-test passes) since the last swr_finish */
 } swr_stats;
 
 /* Context lifetime.  Replaces constructing VertexProcessor(IRasterizer*) + Rasterizer()
@@ -99,6 +101,14 @@ int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
 /* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels. */
 int swr_set_tile_size(swr_context* ctx, int tile);
 const char* swr_status_string(int status);
+
+/* Tracing (no reference counterpart; the reference has only Benchmark.cpp's chrono).
+ * With profiling on, every draw records CUDA events at its stage boundaries on its own
+ * stream; swr_stage_times waits for the draws recorded since its previous call and returns
+ * their summed durations in ms for 5 stages: vertex shading, clip/cull/assembly, triangle
+ * setup, binning, tile raster. */
+int swr_set_profiling(swr_context* ctx, int on);
+int swr_stage_times(swr_context* ctx, float* ms5);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,8 @@ SWR_OK, SWR_EINVAL, SWR_ENOMEM, SWR_EOVERFLOW, SWR_ECUDA, SWR_EINDEX = range(6)
 class SwrStats(ctypes.Structure):
     _fields_ = [("fragments", ctypes.c_uint64), ("primitives", ctypes.c_uint64),
                 ("bin_pairs", ctypes.c_uint64), ("clip_polygons", ctypes.c_uint32),
-                ("flags", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("launches", ctypes.c_uint64),
+                ("passes", ctypes.c_uint64)]
 
 
 class SwrError(RuntimeError):
@@ -54,6 +55,8 @@ def lib():
             "swr_draw_list": [vp, i, vp, u64, vp, u64, vp],
             "swr_finish": [vp, vp, ctypes.POINTER(SwrStats)],
             "swr_set_tile_size": [vp, i],
+            "swr_set_profiling": [vp, i],
+            "swr_stage_times": [vp, ctypes.POINTER(ctypes.c_float)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

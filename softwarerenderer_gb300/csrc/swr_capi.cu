@@ -12,8 +12,9 @@
 
 namespace swr {
 
-// Status buffer: words [0, SWR_ST_WORDS) as in swr_device.cuh; words 8..12 hold the
-// largest per-draw requests seen since the last finish.
+// Status buffer: words [0, SWR_ST_WORDS) as in swr_device.cuh; words 9..13 hold the
+// largest per-draw requests (words 1..5) seen since the last finish; words 14-15 count
+// colour writes.
 constexpr int kStatusWords = 16;
 constexpr int kStickyBase = 8;
 
@@ -80,6 +81,12 @@ struct swr_context {
   swr::Buffer scratch, status, direct_keep, direct_pos;
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
+  // tracing: CUDA events at the stage boundaries of every draw since the last
+  // swr_stage_times call (swr_set_profiling); sextuples reused from a pool
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;  // events recorded (multiple of 6 after a complete draw)
+  uint64_t launches = 0;  // kernels launched since the last swr_finish
 };
 
 namespace {
@@ -90,6 +97,19 @@ int cuda_err(cudaError_t e) {
   if (e == cudaSuccess) return SWR_OK;
   fprintf(stderr, "swr_gb300: CUDA error %s\n", cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? SWR_ENOMEM : SWR_ECUDA;
+}
+
+void mark(swr_context* c, int i, cudaStream_t s) {
+  if (!c->profiling) return;
+  if (i == 0) c->ev_used = (c->ev_used + 5) / 6 * 6;  // start a new sextuple
+  const size_t k = c->ev_used;
+  if (k >= c->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { c->profiling = false; return; }
+    c->ev_pool.push_back(e);
+  }
+  cudaEventRecord(c->ev_pool[k], s);
+  c->ev_used = k + 1;
 }
 
 int bits_for(uint32_t n) {
@@ -183,6 +203,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   sa.tile_count = c->tile_count.as<uint32_t>();
   sa.tile = c->tile;
   ps->setup(sa, s);
+  mark(c, 3, s);
   uint32_t* scr = c->scratch.as<uint32_t>();
   uint32_t* sort_scr = scr + scan_scratch_words(c->cap_prims) + 32;
   scan_exclusive(c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(), st + SWR_ST_PRIMS, c->cap_prims,
@@ -196,6 +217,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   uint32_t* keys = which ? c->keys1.as<uint32_t>() : c->keys0.as<uint32_t>();
   uint32_t* vals = which ? c->vals1.as<uint32_t>() : c->vals0.as<uint32_t>();
   segment_starts(keys, st + SWR_ST_PAIRS, c->cap_pairs, ntiles, c->tile_start.as<uint32_t>(), s);
+  mark(c, 4, s);
   RasterArgs ra;
   ra.status = st;
   ra.tile_start = c->tile_start.as<uint32_t>();
@@ -207,7 +229,10 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.ntargets = 1;
   ra.status_w = st;
   ps->raster(ra, ntiles, c->tile, s);
+  mark(c, 5, s);
   k_close_draw<<<1, 1, 0, s>>>(st);
+  const int passes = (bits_for(ntiles) + 7) / 8;
+  c->launches += 1 + 3 + 1 + 5 * passes + 1 + (ntiles ? 1 : 0) + 1;
   return cuda_err(cudaGetLastError());
 }
 
@@ -259,6 +284,7 @@ int swr_create(swr_context** out) {
 int swr_destroy(swr_context* c) {
   if (!c) return SWR_EINVAL;
   if (c->status_host) cudaFreeHost(c->status_host);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   delete c;
   return SWR_OK;
 }
@@ -359,7 +385,10 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   D.nprims = nsub;
   if ((rc = upload_single(c, D, T, s))) return rc;
   uint32_t* st = c->status.as<uint32_t>();
+  mark(c, 0, s);
   vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts, c->ptv.as<float>(), s);
+  mark(c, 1, s);
+  c->launches += (nverts ? 1 : 0) + (nbatches ? 2 : 0) + 1;
   AssembleArgs aa;
   aa.draws = c->draws.as<SwrDrawDesc>();
   aa.ndraws = 1;
@@ -380,6 +409,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
                                   c->cap_prims);
   vs->assemble_emit(aa, nbatches, s);
+  mark(c, 2, s);
   c->last_ntiles = ntiles;
   return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s);
 }
@@ -407,7 +437,10 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   D.nverts = (uint32_t)nverts;
   if ((rc = upload_single(c, D, T, s))) return rc;
   uint32_t* st = c->status.as<uint32_t>();
+  mark(c, 0, s);
   ps->direct_vertices(vertices, (uint32_t)nverts, c->ptv.as<float>(), s);
+  mark(c, 1, s);
+  c->launches += (nverts ? 1 : 0) + (nsub ? 5 : 0);
   if (nsub) {
     const int grid = (int)((nsub + 255) / 256 < 1216 ? (nsub + 255) / 256 : 1216);
     k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, 3, c->direct_keep.as<uint32_t>());
@@ -416,6 +449,7 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
     k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, 3, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
                                        c->direct_pos.as<uint32_t>(), c->tris.as<uint4>(), st);
   }
+  mark(c, 2, s);
   c->last_ntiles = ntiles;
   return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s);
 }
@@ -433,7 +467,10 @@ int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
     stats->bin_pairs = h[SWR_ST_PAIRS];
     stats->clip_polygons = h[SWR_ST_CLIP_SLOTS];
     stats->flags = h[SWR_ST_FLAGS];
+    stats->launches = c->launches;
+    stats->passes = (uint64_t)h[SWR_ST_PASSES_LO] | ((uint64_t)h[SWR_ST_PASSES_HI] << 32);
   }
+  c->launches = 0;
   const uint32_t flags = h[SWR_ST_FLAGS];
   if (flags & SWR_F_ANY_OVERFLOW) {
     grow_u32(c->cap_clip_slots, h[kStickyBase + SWR_ST_CLIP_SLOTS]);
@@ -446,6 +483,29 @@ int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
   if (flags & SWR_F_ANY_OVERFLOW) return SWR_EOVERFLOW;
   if (flags & SWR_F_BAD_INDEX) return SWR_EINDEX;
   return SWR_OK;
+}
+
+int swr_set_profiling(swr_context* c, int on) {
+  if (!c) return SWR_EINVAL;
+  c->profiling = on != 0;
+  c->ev_used = 0;
+  return SWR_OK;
+}
+
+int swr_stage_times(swr_context* c, float* ms) {
+  if (!c || !ms) return SWR_EINVAL;
+  for (int i = 0; i < 5; ++i) ms[i] = 0.0f;
+  const size_t draws = c->ev_used / 6;
+  int rc = SWR_OK;
+  if (draws) rc = cuda_err(cudaEventSynchronize(c->ev_pool[6 * draws - 1]));
+  for (size_t d = 0; d < draws && !rc; ++d)
+    for (int i = 0; i < 5; ++i) {
+      float t = 0.0f;
+      if ((rc = cuda_err(cudaEventElapsedTime(&t, c->ev_pool[6 * d + i], c->ev_pool[6 * d + i + 1])))) break;
+      ms[i] += t;
+    }
+  c->ev_used = 0;
+  return rc;
 }
 
 const char* swr_status_string(int st) {

@@ -18,7 +18,9 @@ enum SwrStatusWord {
   SWR_ST_FRAGS = 5,       // line/point fragments requested
   SWR_ST_SHADED_LO = 6,   // drawPixel calls (64-bit, low word)
   SWR_ST_SHADED_HI = 7,
-  SWR_ST_WORDS = 8
+  SWR_ST_WORDS = 8,
+  SWR_ST_PASSES_LO = 14,  // colour writes (depth-test passes), 64-bit (8-byte aligned), sticky
+  SWR_ST_PASSES_HI = 15
 };
 
 enum SwrStatusFlags {

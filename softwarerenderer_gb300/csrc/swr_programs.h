@@ -13,7 +13,10 @@
 //
 // Pixel shader contract: static AVarCount, PVarCount, InterpolateZ, InterpolateW
 // (PixelShaderBase.h:44-53), a per-pixel State that the reference keeps in the
-// shader's own static buffers, and load / drawPixel / store.  drawPixel is the
+// shader's own static buffers (with `frags` and `writes` counters), and
+// load / drawPixel / store / earlyReject.  earlyReject(z, s) returns true when
+// drawPixel with depth z would do nothing but count the fragment (a failing depth test);
+// it then counts it itself, so the rasterizer may skip building the other interpolants.  drawPixel is the
 // reference's drawPixel(const PixelData&) (PixelShaderBase.h:116); load/store move
 // the pixel's framebuffer values between memory and State.  Calling
 // load + drawPixel + store per fragment is exactly the reference's side effect; the
@@ -160,6 +163,15 @@ struct SwrStateRGBA32F {
   int32_t winner;
 };
 
+// Early depth rejection shared by the depth-tested shaders: their drawPixel does only
+// `s.frags++` when !(z < s.depth).
+template <class State>
+SWR_HD bool swr_depth_reject(float z, State& s) {
+  if (z < s.depth) return false;
+  s.frags++;
+  return true;
+}
+
 template <bool kDepth>
 SWR_HD void swr_load_rgba8(SwrStateRGBA8& s, int x, int y, const SwrUniforms& u) {
   const size_t i = (size_t)y * (size_t)u.width + (size_t)x;
@@ -196,6 +208,7 @@ struct PsTexNearest {
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
@@ -215,6 +228,7 @@ struct PsLambert {
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
   SWR_HD static float intensity(float n0, float n1, float n2, const SwrUniforms& u) {
     const float len2 = swr_add(swr_add(swr_mul(n0, n0), swr_mul(n1, n1)), swr_mul(n2, n2));
     float d = 0.0f;
@@ -251,6 +265,7 @@ struct PsLambertTex {
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
@@ -273,6 +288,7 @@ struct PsVColor {
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
@@ -293,6 +309,7 @@ struct PsVColorAffine {
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<false>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, false); }
+  SWR_HD static bool earlyReject(float, State&) { return false; }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
@@ -340,6 +357,7 @@ struct PsDiff {
     s.writes = 0u;
     s.winner = -1;
   }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) {
     const size_t i = (size_t)y * (size_t)u.width + (size_t)x;
     if (s.writes) {

@@ -731,11 +731,80 @@ struct RasterArgs {
   uint32_t* status_w;
 };
 
+// v <- fl(v + a) repeated k times for 0 <= k <= 7 (steps inside one 8x8 block), as
+// predicated adds so the lanes of a warp never diverge.
+__device__ __forceinline__ float fold7(float v, float a, int k) {
+#pragma unroll
+  for (int i = 0; i < 7; ++i) v = i < k ? swr_add(v, a) : v;
+  return v;
+}
+
+// Exact 8x8 coverage mask of one block (Rasterizer.h:263-304 classification, then
+// PixelShaderBase::drawBlock<TestEdges> per-pixel tests with EdgeData stepping,
+// PixelShaderBase.h:64-93): bit r*8+c set when pixel (bx+c, by+r) reaches drawPixel.
+__device__ __forceinline__ uint64_t block_mask(const float* r, int flags, int bx, int by) {
+  const float fx = swr_add((float)bx, 0.5f), fy = swr_add((float)by, 0.5f);
+  const float s = (float)(SWR_BLOCK - 1);
+  float ev[3];
+  bool t00[3], t01[3], t10[3], t11[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float ea = r[6 + 3 * j], eb = r[7 + 3 * j], ec = r[8 + 3 * j];
+    const bool tie = (flags >> (2 + j)) & 1;
+    ev[j] = swr_eval(ea, eb, ec, fx, fy);
+    const float v01 = swr_add(ev[j], swr_mul(eb, s));
+    const float v10 = swr_add(ev[j], swr_mul(ea, s));
+    const float v11 = swr_add(v01, swr_mul(ea, s));
+    t00[j] = edge_test(ev[j], tie);
+    t01[j] = edge_test(v01, tie);
+    t10[j] = edge_test(v10, tie);
+    t11[j] = edge_test(v11, tie);
+  }
+  const int inside = (t00[0] && t00[1] && t00[2]) + (t01[0] && t01[1] && t01[2]) +
+                     (t10[0] && t10[1] && t10[2]) + (t11[0] && t11[1] && t11[2]);
+  if (inside == 4) return ~0ull;  // drawBlock<false>: every pixel
+  if (inside == 0) {
+    const bool s00 = (t00[0] == t00[1]) == t00[2], s01 = (t01[0] == t01[1]) == t01[2];
+    const bool s10 = (t10[0] == t10[1]) == t10[2], s11 = (t11[0] == t11[1]) == t11[2];
+    if (s00 && s01 && s10 && s11) return 0ull;  // skipped
+  }
+  // drawBlock<true>: row starts step by b, pixels step by a
+  const bool tie0 = (flags >> 2) & 1, tie1 = (flags >> 3) & 1, tie2 = (flags >> 4) & 1;
+  float o0 = ev[0], o1 = ev[1], o2 = ev[2];
+  uint64_t m = 0;
+  for (int row = 0; row < SWR_BLOCK; ++row) {
+    float i0 = o0, i1 = o1, i2 = o2;
+#pragma unroll
+    for (int col = 0; col < SWR_BLOCK; ++col) {
+      if (edge_test(i0, tie0) && edge_test(i1, tie1) && edge_test(i2, tie2)) m |= 1ull << (row * 8 + col);
+      i0 = swr_add(i0, r[6]);
+      i1 = swr_add(i1, r[9]);
+      i2 = swr_add(i2, r[12]);
+    }
+    o0 = swr_add(o0, r[7]);
+    o1 = swr_add(o1, r[10]);
+    o2 = swr_add(o2, r[13]);
+  }
+  return m;
+}
+
+// One CTA per screen tile, 256 threads.  Per chunk of CH primitives of the tile's bin:
+//   A. stage the setup records in shared memory;
+//   B. one thread per (primitive, 8x8 block) computes the block's exact coverage mask and
+//      one thread per (primitive, tile row) the row's span ends [xl, xr);
+//   C. each thread walks the chunk in primitive order for the pixels it owns, tests
+//      coverage with one bit / one range, rebuilds the incrementally stepped interpolants
+//      of covered pixels (z first: a failing depth test needs nothing else) and calls the
+//      pixel shader on the pixel's register-resident State.
 template <class PS, int TILE, int CH>
 __global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
   typedef Rec<PS> RL;
   constexpr int PPT = TILE * TILE / 256;  // pixels per thread
+  constexpr int NBX = TILE / SWR_BLOCK;   // blocks per tile row
+  constexpr int NB = NBX * NBX;
   __shared__ float srec[CH * RL::R];
+  __shared__ uint64_t smask[CH * NB];
+  __shared__ int2 sspan[CH * TILE];
   __shared__ uint32_t sids[CH];
   __shared__ uint32_t sfr[32];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
@@ -747,18 +816,20 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
   const SwrUniforms& U = g.draws[T.first_draw].u;
   const uint32_t lt = tile - T.tile_base;
   const int ox = (int)(lt % (uint32_t)T.tiles_x) * TILE, oy = (int)(lt / (uint32_t)T.tiles_x) * TILE;
-  // Thread -> pixels: each warp covers an 8 x 4 half block; sub-tiles of 16 x 16 repeat.
+  // Thread -> pixels: each warp covers an 8 x 4 half block; 16 x 16 sub-tiles repeat.
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int px[PPT], py[PPT];
+  int px[PPT], py[PPT], blk[PPT];
   bool in[PPT];
   typename PS::State st[PPT];
 #pragma unroll
   for (int q = 0; q < PPT; ++q) {
-    const int sub = q;  // 16x16 sub-tile index
-    const int sxo = (sub % (TILE / 16)) * 16, syo = (sub / (TILE / 16)) * 16;
-    const int blk = warp >> 1;
-    px[q] = ox + sxo + (blk & 1) * 8 + (lane & 7);
-    py[q] = oy + syo + (blk >> 1) * 8 + (warp & 1) * 4 + (lane >> 3);
+    const int sxo = (q % (TILE / 16)) * 16, syo = (q / (TILE / 16)) * 16;
+    const int hb = warp >> 1;
+    const int lx = sxo + (hb & 1) * 8 + (lane & 7);
+    const int ly = syo + (hb >> 1) * 8 + (warp & 1) * 4 + (lane >> 3);
+    px[q] = ox + lx;
+    py[q] = oy + ly;
+    blk[q] = (ly >> 3) * NBX + (lx >> 3);
     in[q] = px[q] < T.width && py[q] < T.height;
     if (in[q]) PS::load(st[q], px[q], py[q], U);
   }
@@ -773,75 +844,67 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
       srec[i] = g.recs[(size_t)sids[k] * RL::R + w];
     }
     __syncthreads();
+    // B: coverage per (primitive, block) and per (primitive, row)
+    for (int i = threadIdx.x; i < n * NB; i += 256) {
+      const int k = i / NB, j = i - k * NB;
+      const float* r = srec + k * RL::R;
+      const int flags = __float_as_int(r[0]);
+      const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
+      uint64_t m = 0;
+      if ((flags & 3) == 3 && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
+          by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]))
+        m = block_mask(r, flags, bx, by);
+      smask[i] = m;
+    }
+    for (int i = threadIdx.x; i < n * TILE; i += 256) {
+      const int k = i / TILE, row = i - k * TILE;
+      const float* r = srec + k * RL::R;
+      const int flags = __float_as_int(r[0]);
+      const int y = oy + row;
+      int2 sp = make_int2(1, 0);
+      if ((flags & 3) == 1 && y >= __float_as_int(r[3]) && y <= __float_as_int(r[5])) {
+        SpanHalf h;
+        bool any = true;
+        if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
+          h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
+        } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
+          h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
+        } else {
+          any = false;
+        }
+        if (any) {
+          const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+          span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
+        }
+      }
+      sspan[i] = sp;
+    }
+    __syncthreads();
+    // C: fragments in primitive order
     for (int k = 0; k < n; ++k) {
       const float* r = srec + k * RL::R;
       const int flags = __float_as_int(r[0]);
-      const int x0 = __float_as_int(r[2]), y0 = __float_as_int(r[3]);
-      const int x1 = __float_as_int(r[4]), y1 = __float_as_int(r[5]);
-      const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+      if (!(flags & 1)) continue;
+      const bool blockmode = flags & 2;
       const float* eq = r + RL::EQ0;
 #pragma unroll
       for (int q = 0; q < PPT; ++q) {
-        if (!in[q] || px[q] < x0 || px[q] > x1 || py[q] < y0 || py[q] > y1) continue;
+        if (!in[q]) continue;
         float fx, fy;
-        int ka, kb;  // steps along a (x) and b (y) from the evaluation point
-        if (flags & 2) {
-          const int bx = px[q] & ~(SWR_BLOCK - 1), by = py[q] & ~(SWR_BLOCK - 1);
-          fx = swr_add((float)bx, 0.5f);
-          fy = swr_add((float)by, 0.5f);
-          bool t00[3], t01[3], t10[3], t11[3];
-          float ev[3];
-          const float s = (float)(SWR_BLOCK - 1);
-#pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            const float ea = r[6 + 3 * j], eb = r[7 + 3 * j], ec = r[8 + 3 * j];
-            const bool tie = (flags >> (2 + j)) & 1;
-            ev[j] = swr_eval(ea, eb, ec, fx, fy);
-            const float v01 = swr_add(ev[j], swr_mul(eb, s));
-            const float v10 = swr_add(ev[j], swr_mul(ea, s));
-            const float v11 = swr_add(v01, swr_mul(ea, s));
-            t00[j] = edge_test(ev[j], tie);
-            t01[j] = edge_test(v01, tie);
-            t10[j] = edge_test(v10, tie);
-            t11[j] = edge_test(v11, tie);
-          }
-          const int inside = (t00[0] && t00[1] && t00[2]) + (t01[0] && t01[1] && t01[2]) +
-                             (t10[0] && t10[1] && t10[2]) + (t11[0] && t11[1] && t11[2]);
-          kb = py[q] - by;
-          ka = px[q] - bx;
-          bool test = true;
-          if (inside == 0) {
-            const bool s00 = (t00[0] == t00[1]) == t00[2], s01 = (t01[0] == t01[1]) == t01[2];
-            const bool s10 = (t10[0] == t10[1]) == t10[2], s11 = (t11[0] == t11[1]) == t11[2];
-            if (s00 && s01 && s10 && s11) continue;
-          } else if (inside == 4) {
-            test = false;
-          }
-          if (test) {
-            bool ok = true;
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-              const float v = swr_fold(swr_fold(ev[j], r[7 + 3 * j], kb), r[6 + 3 * j], ka);
-              ok = ok && edge_test(v, (flags >> (2 + j)) & 1);
-            }
-            if (!ok) continue;
-          }
+        int ka, kb;
+        if (blockmode) {
+          const uint64_t m = smask[k * NB + blk[q]];
+          if (!((m >> ((py[q] & 7) * 8 + (px[q] & 7))) & 1ull)) continue;
+          fx = swr_add((float)(px[q] & ~7), 0.5f);
+          fy = swr_add((float)(py[q] & ~7), 0.5f);
+          ka = px[q] & 7;
+          kb = py[q] & 7;
         } else {
-          int xl, xr;
-          SpanHalf h;
-          const int y = py[q];
-          if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
-            h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
-          } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
-            h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
-          } else {
-            continue;
-          }
-          span_row(h, y, D.sc_minx, D.sc_maxx, xl, xr);
-          if (px[q] < xl || px[q] >= xr) continue;
-          fx = swr_add((float)xl, 0.5f);
-          fy = swr_add((float)y, 0.5f);
-          ka = px[q] - xl;
+          const int2 sp = sspan[k * TILE + (py[q] - oy)];
+          if (px[q] < sp.x || px[q] >= sp.y) continue;
+          fx = swr_add((float)sp.x, 0.5f);
+          fy = swr_add((float)py[q], 0.5f);
+          ka = px[q] - sp.x;
           kb = 0;
         }
         GpuPixel<PS> pd;
@@ -849,38 +912,50 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
         pd.y = py[q];
         if (RL::IZ) {
           const float* q3 = eq + 3 * RL::EQ_Z;
-          pd.z = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          const float z0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+          pd.z = blockmode ? fold7(z0, q3[0], ka) : swr_fold(z0, q3[0], ka);
+          frags++;
+          if (PS::earlyReject(pd.z, st[q])) continue;
+        } else {
+          frags++;
         }
         if (RL::IW) {
           const float* q3 = eq + 3 * RL::EQ_W;
-          pd.invw = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+          pd.invw = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
           pd.w = swr_div(1.0f, pd.invw);
         }
 #pragma unroll
         for (int i = 0; i < RL::NA; ++i) {
           const float* q3 = eq + 3 * (RL::EQ_A + i);
-          pd.avar[i] = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+          pd.avar[i] = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
         }
 #pragma unroll
         for (int i = 0; i < RL::NP; ++i) {
           const float* q3 = eq + 3 * (RL::EQ_P + i);
-          const float pt = swr_fold(swr_fold(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb), q3[0], ka);
+          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+          const float pt = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
           pd.pvar[i] = swr_mul(pt, pd.w);
         }
-        PS::drawPixel(pd, (int)sids[k], st[q], D.u);
-        frags++;
+        PS::drawPixel(pd, (int)sids[k], st[q], g.draws[__float_as_int(r[1])].u);
       }
     }
   }
+  uint32_t passes = 0;
 #pragma unroll
   for (int q = 0; q < PPT; ++q)
-    if (in[q]) PS::store(st[q], px[q], py[q], U);
-  // fragment statistics
-  uint32_t tot;
+    if (in[q]) {
+      PS::store(st[q], px[q], py[q], U);
+      passes += st[q].writes;
+    }
+  // fragment statistics: drawPixel calls and colour writes
+  uint32_t tot, ptot;
   swr_block_exscan(frags, sfr, &tot);
+  swr_block_exscan(passes, sfr, &ptot);
   if (threadIdx.x == 0 && tot) {
-    const unsigned long long old = atomicAdd((unsigned long long*)&g.status_w[SWR_ST_SHADED_LO], (unsigned long long)tot);
-    (void)old;
+    atomicAdd((unsigned long long*)&g.status_w[SWR_ST_SHADED_LO], (unsigned long long)tot);
+    atomicAdd((unsigned long long*)&g.status_w[SWR_ST_PASSES_LO], (unsigned long long)ptot);
   }
 }
 

@@ -51,7 +51,20 @@ class Context:
         st = _lib.SwrStats()
         rc = self.L.swr_finish(self.h, _stream(), ctypes.byref(st))
         return rc, {"fragments": st.fragments, "primitives": st.primitives,
-                    "bin_pairs": st.bin_pairs, "clip_polygons": st.clip_polygons, "flags": st.flags}
+                    "bin_pairs": st.bin_pairs, "clip_polygons": st.clip_polygons, "flags": st.flags,
+                    "launches": st.launches, "passes": st.passes}
+
+    def set_profiling(self, on=True):
+        _lib.check(self.L.swr_set_profiling(self.h, int(bool(on))), "set_profiling")
+
+    STAGES = ("vertex", "assemble", "setup", "bin", "raster")
+
+    def stage_times(self):
+        """Per-stage durations (ms) summed over the draws since the previous call, measured
+        with CUDA events on the stream the stage kernels run on."""
+        ms = (ctypes.c_float * 5)()
+        _lib.check(self.L.swr_stage_times(self.h, ms), "stage_times")
+        return dict(zip(self.STAGES, [float(x) for x in ms]))
 
 
 class Rasterizer:
