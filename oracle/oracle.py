@@ -66,6 +66,9 @@ def load(which="port"):
         lib.oracle_draw.restype = ctypes.c_int
         lib.oracle_fold.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int]
         lib.oracle_fold.restype = ctypes.c_float
+        if hasattr(lib, "oracle_fold_selftest"):
+            lib.oracle_fold_selftest.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+            lib.oracle_fold_selftest.restype = ctypes.c_uint64
         _LIBS[which] = Oracle(lib, which)
     return _LIBS[which]
 

@@ -43,6 +43,8 @@ typedef struct OracleStats {
 int oracle_draw(const OracleDraw* d, OracleStats* st);
 /* swr_fold exposed for the tests of the fast-forward. */
 float oracle_fold(float v, float a, int k);
+/* Randomized comparison of swr_fold with serial stepping; returns the mismatch count. */
+uint64_t oracle_fold_selftest(uint64_t iters, uint64_t seed);
 
 #ifdef __cplusplus
 }

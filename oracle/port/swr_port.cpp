@@ -11,6 +11,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include <vector>
 #include <utility>
 #include "../oracle_abi.h"
@@ -686,3 +687,51 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
 }
 
 extern "C" float oracle_fold(float v, float a, int k) { return swr_fold(v, a, k); }
+
+// Randomized check of swr_fold against plain serial stepping: returns the number of
+// (v, a, k) cases where they differ (NaN results compare equal).  Cases mix arbitrary bit
+// patterns, moderate magnitudes, powers of two and their neighbours (binade edges),
+// subnormals, and increments placed on or next to half-ulp ties of v.
+extern "C" uint64_t oracle_fold_selftest(uint64_t iters, uint64_t seed) {
+  uint64_t s = seed * 0x9E3779B97F4A7C15ull + 88172645463325252ull;
+  auto rnd = [&]() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; };
+  auto bits = [](uint32_t b) { float f; memcpy(&f, &b, 4); return f; };
+  auto pick = [&]() -> float {
+    switch (rnd() % 7) {
+      case 0: return bits((uint32_t)rnd());
+      case 1: return bits(((uint32_t)rnd() & 0x807fffffu) | ((uint32_t)(100 + rnd() % 56) << 23));
+      case 2: return (float)((double)(rnd() % 2000001) / 1000.0 - 1000.0);
+      case 3: {
+        float f = bits((uint32_t)(97 + rnd() % 60) << 23);
+        if (rnd() & 1) f = -f;
+        uint32_t b; memcpy(&b, &f, 4);
+        b += (uint32_t)(rnd() % 3) - 1;
+        return bits(b);
+      }
+      case 4: return bits(((uint32_t)rnd() & 0x80000000u) | (uint32_t)(rnd() % 64));
+      case 5: return (float)((double)((int)(rnd() % 200001) - 100000) / (double)(1u << (rnd() % 30)));
+      default: return bits(((uint32_t)rnd() & 0x807fffffu) | ((uint32_t)(110 + rnd() % 30) << 23));
+    }
+  };
+  uint64_t bad = 0;
+  for (uint64_t it = 0; it < iters; ++it) {
+    float v = pick(), a = pick();
+    if (rnd() % 4 == 0) {  // increments of (q + 1/2 or q + f) ulps of v: ties and near-ties
+      uint32_t vb; memcpy(&vb, &v, 4);
+      const int e = (int)((vb >> 23) & 0xff) - 150;
+      const double u = e > -150 ? ldexp(1.0, e) : ldexp(1.0, -149);
+      const double q = (double)(rnd() % 64) + ((rnd() & 1) ? 0.5 : (double)(rnd() % 1000) / 1000.0);
+      a = (float)(q * u * (double)(1u << (rnd() % 5)));
+      if (rnd() & 1) a = -a;
+    }
+    const int k = (int)(rnd() % ((rnd() % 3 == 0) ? 5000 : 300));
+    float ref = v;
+    for (int i = 0; i < k; ++i) ref = ref + a;
+    const float got = swr_fold(v, a, k);
+    uint32_t rb, gb;
+    memcpy(&rb, &ref, 4);
+    memcpy(&gb, &got, 4);
+    if (rb != gb && !(ref != ref && got != got)) bad++;
+  }
+  return bad;
+}
