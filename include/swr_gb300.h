@@ -110,6 +110,26 @@ const char* swr_status_string(int status);
 int swr_set_profiling(swr_context* ctx, int on);
 int swr_stage_times(swr_context* ctx, float* ms5);
 
+/* Allocation-free triangle-list draw.  No counterpart in the reference (whose CPU
+ * rasterizer needs no device scratch).  It is swr_draw_list(SWR_DRAW_TRIANGLE, ...) for
+ * callers that must not allocate device memory -- an application whose device memory is
+ * owned by another allocator or capped at start-up, a frame loop that must not stall in
+ * the driver's allocator, a plugin handed only a stream and target buffers -- so it takes
+ * its state as arguments instead of a swr_context (creating one allocates) and keeps all
+ * scratch in one fixed 8 MiB __device__ array inside the library.  It calls no cudaMalloc
+ * or cudaFree.  Limits: <= 4096 triangles, <= 12288 vertices, a target of <= 16384 tiles
+ * of 16 x 16 pixels (e.g. 2048 x 2048); larger inputs return SWR_EINVAL up front, and more
+ * than 262144 (tile, triangle) bin entries return SWR_EOVERFLOW with the target untouched.
+ * Synchronous: returns after the stream has drained; *fragments (may be NULL) receives
+ * the drawPixel count.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and must come before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them. */
+int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int ps_id, int raster_mode,
+                                   int scissor_x, int scissor_y, int scissor_w, int scissor_h,
+                                   const float* vertices, uint64_t nverts,
+                                   const int32_t* indices, uint64_t count, void* stream,
+                                   uint64_t* fragments);
+
 #ifdef __cplusplus
 }
 #endif
