@@ -169,6 +169,19 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
+def reduce_replicas(ms, frags, dist=None, device="cpu"):
+    """Whole-job timing of independent replicas: the slowest rank's time and the fragments
+    of all ranks (no collective touches the rendering itself)."""
+    if dist is None:
+        return float(ms), float(frags)
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    f = torch.tensor([frags], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(f, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(f[0])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -244,15 +257,7 @@ def main():
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     ms_max = ms
     frags, passes = st["fragments"], st["passes"]
-    if dist:
-        t = torch.tensor([ms, frags], dtype=torch.float64, device="cuda")
-        tm = t.clone()
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_max = float(tm[0])
-        frags_all = float(t[1])
-    else:
-        frags_all = float(frags)
+    ms_max, frags_all = reduce_replicas(ms, frags, dist, "cuda")
     value = frags_all / (ms_max / 1e3) / 1e9
     mtris = 327680 * args.steps * world / (ms_max / 1e3) / 1e6
 

@@ -434,3 +434,58 @@ def random_scene(seed: int, direct: Optional[bool] = None, draw_mode: Optional[D
                  cull=cull, raster=raster, viewport=viewport, depth_range=depth_range,
                  scissor=scissor, attribs=attribs, indices=idx, mvp=mvp, light=light,
                  texture=tex, checker=int(rng.integers(2, 20)))
+
+
+# ----------------------------------------------------------------------------
+# Benchmark.cpp-shaped scene and spec-driven construction (fixtures, tests, bench)
+
+def benchmark_scene(n_tris: int = 4096 * 10, seed: int = 0) -> Scene:
+    """The shape of the reference's own benchmark scene (Benchmark.cpp:66-105): 40,960
+    triangles of three fresh vertices each with x, y, z and r, g, b uniform in [0, 1), w = 1
+    (identity transform), 640x480 viewport and scissor, CullMode None, default Span mode,
+    an affine-colour pixel shader without depth test.  Values come from numpy's PCG64
+    rather than the reference's Random class."""
+    rng = np.random.default_rng(seed)
+    v = rng.random((3 * n_tris, 6)).astype(np.float32)
+    return Scene(name=f"benchmark{n_tris}", vs=VS.POS_RGB_AFFINE, ps=PS.VCOLOR_AFFINE, width=640,
+                 height=480, cull=CullMode.None_, raster=RasterMode.Span, viewport=(0, 0, 640, 480),
+                 scissor=(0, 0, 640, 480), attribs=[(v, 24)],
+                 indices=np.arange(3 * n_tris, dtype=np.int32))
+
+
+def scene_from_spec(spec: dict) -> Scene:
+    k = spec["kind"]
+    if k == "random":
+        dm = spec.get("draw_mode")
+        return random_scene(spec["seed"], direct=spec.get("direct"),
+                            draw_mode=DrawMode(dm) if dm is not None else None,
+                            n_prims=spec.get("n_prims"))
+    if k == "cube":
+        return cube_scene(spec["frame"])
+    if k == "sphere":
+        return sphere_scene(spec["pose"], level=spec.get("level", 7), width=spec.get("width", 1920),
+                            height=spec.get("height", 1080), raster=RasterMode(spec.get("raster", 1)))
+    if k == "soup":
+        return soup_scene(spec["n"], width=spec.get("width", 3840), height=spec.get("height", 2160),
+                          raster=RasterMode(spec.get("raster", 2)))
+    if k == "benchmark":
+        return benchmark_scene(spec.get("n", 4096 * 10))
+    raise ValueError(k)
+
+
+def scene_digest(scene: Scene) -> str:
+    """SHA-256 (32 hex digits) of every input of a scene: proves that a scene rebuilt from
+    its spec on another machine is bit-identical to the one a fixture was made from."""
+    import hashlib
+    h = hashlib.sha256()
+    for a, s in scene.attribs:
+        h.update(np.ascontiguousarray(a).tobytes())
+        h.update(str(s).encode())
+    for a in (scene.indices, scene.raster_vertices, scene.mvp, scene.light, scene.texture):
+        if a is not None:
+            h.update(np.ascontiguousarray(a).tobytes())
+    h.update(repr((int(scene.vs), int(scene.ps), scene.width, scene.height, int(scene.draw_mode),
+                   int(scene.cull), int(scene.raster), tuple(scene.viewport),
+                   tuple(float(x) for x in scene.depth_range), tuple(scene.scissor),
+                   scene.checker)).encode())
+    return h.hexdigest()[:32]
