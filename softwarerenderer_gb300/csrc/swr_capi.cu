@@ -78,7 +78,7 @@ struct swr_context {
   swr::Buffer draws, targets, draw_vbase, draw_bbase, target_tile_base;
   swr::Buffer ptv, clipv, clip_table, clip_slot, tri_flags, batch_counts, batch_base;
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
-  swr::Buffer scratch, status, direct_keep, direct_pos;
+  swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs;
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
   // tracing: CUDA events at the stage boundaries of every draw since the last
@@ -139,6 +139,7 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->clip_table.ensure((size_t)c->cap_clip_slots * sizeof(SwrClipEntry) + 16);
   ok &= c->clip_slot.ensure((size_t)nsub * 4 + 16);
   ok &= c->tri_flags.ensure((size_t)nsub + 16);
+  ok &= c->lp_refs.ensure((size_t)nsub * 8 + 16);
   ok &= c->batch_counts.ensure((size_t)nbatches * 8 + 16);
   ok &= c->batch_base.ensure((size_t)nbatches * 4 + 16);
   ok &= c->tris.ensure((size_t)c->cap_prims * 16 + 16);
@@ -233,6 +234,75 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   k_close_draw<<<1, 1, 0, s>>>(st);
   const int passes = (bits_for(ntiles) + 7) / 8;
   c->launches += 1 + 3 + 1 + 5 * passes + 1 + (ntiles ? 1 : 0) + 1;
+  return cuda_err(cudaGetLastError());
+}
+
+// Points and lines: per-primitive DDA setup, one fragment per step, stable sort by pixel,
+// per-pixel ordered shading.  Fragment buffers reuse the bin-pair queues.
+int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int vs_a, int vs_p,
+             const SwrTargetDesc& T, cudaStream_t s) {
+  uint32_t* st = c->status.as<uint32_t>();
+  SetupArgs sa;
+  memset(&sa, 0, sizeof(sa));
+  sa.tris = c->tris.as<uint4>();
+  sa.status = st;
+  sa.cap_prims = c->cap_prims;
+  sa.ptv = c->ptv.as<float>();
+  sa.clipv = c->clipv.as<float>();
+  sa.S = S;
+  sa.off_a = off_a;
+  sa.off_p = off_p;
+  sa.vs_a = vs_a;
+  sa.vs_p = vs_p;
+  sa.draws = c->draws.as<SwrDrawDesc>();
+  sa.targets = c->targets.as<SwrTargetDesc>();
+  sa.recs = c->recs.as<float>();
+  sa.tile_count = c->tile_count.as<uint32_t>();
+  sa.tile = c->tile;
+  ps->lp_setup(sa, s);
+  mark(c, 3, s);
+  uint32_t* scr = c->scratch.as<uint32_t>();
+  uint32_t* sort_scr = scr + scan_scratch_words(c->cap_prims) + 32;
+  scan_exclusive(c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(), st + SWR_ST_PRIMS, c->cap_prims,
+                 st + SWR_ST_PAIRS, scr, s);
+  const uint32_t invalid = (uint32_t)T.width * (uint32_t)T.height;
+  LpFragArgs fa;
+  fa.status = st;
+  fa.cap_prims = c->cap_prims;
+  fa.recs = c->recs.as<float>();
+  fa.frag_off = c->pair_off.as<uint32_t>();
+  fa.nfrags = st + SWR_ST_PAIRS;
+  fa.cap_frags = c->cap_pairs;
+  fa.draws = c->draws.as<SwrDrawDesc>();
+  fa.targets = c->targets.as<SwrTargetDesc>();
+  fa.keys = c->keys0.as<uint32_t>();
+  fa.vals = c->vals0.as<uint32_t>();
+  fa.status_w = st;
+  fa.invalid = invalid;
+  ps->lp_frags(fa, s);
+  const int bits = bits_for(invalid + 1);
+  const int which = radix_sort_pairs(c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), c->keys1.as<uint32_t>(),
+                                     c->vals1.as<uint32_t>(), st + SWR_ST_PAIRS, c->cap_pairs, bits, sort_scr, s);
+  mark(c, 4, s);
+  LpShadeArgs sh;
+  sh.status = st;
+  sh.cap_prims = c->cap_prims;
+  sh.recs = c->recs.as<float>();
+  sh.frag_off = c->pair_off.as<uint32_t>();
+  sh.nfrags = st + SWR_ST_PAIRS;
+  sh.cap_frags = c->cap_pairs;
+  sh.keys = which ? c->keys1.as<uint32_t>() : c->keys0.as<uint32_t>();
+  sh.vals = which ? c->vals1.as<uint32_t>() : c->vals0.as<uint32_t>();
+  sh.draws = c->draws.as<SwrDrawDesc>();
+  sh.targets = c->targets.as<SwrTargetDesc>();
+  sh.target_pixel_base = c->target_tile_base.as<uint32_t>();
+  sh.ntargets = 1;
+  sh.invalid = invalid;
+  sh.status_w = st;
+  ps->lp_shade(sh, s);
+  mark(c, 5, s);
+  k_close_draw<<<1, 1, 0, s>>>(st);
+  c->launches += 1 + 3 + 1 + 5 * ((bits + 7) / 8) + 1 + 1;
   return cuda_err(cudaGetLastError());
 }
 
@@ -357,8 +427,9 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   const VsOps* vs = vs_ops(c->vs_id);
   const PsOps* ps = ps_ops(c->ps_id);
   if (!vs || !ps) return SWR_EINVAL;
-  if (mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // points and lines: see swr_lines.cu
-  if (count % 3 || count / 3 >= 0x7fffffffull || (count && !indices)) return SWR_EINVAL;
+  if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
+  const uint64_t per = mode == SWR_DRAW_POINT ? 1 : (mode == SWR_DRAW_LINE ? 2 : 3);
+  if (count % per || count / per >= 0x7fffffffull || (count && !indices)) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   uint64_t nverts = ~0ull;
   for (int a = 0; a < vs->attribs; ++a) {
@@ -371,11 +442,11 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   }
   if (vs->attribs == 0) nverts = 0;
   if (nverts >= 0x7fffffffull) return SWR_EINVAL;
-  const uint32_t nsub = (uint32_t)(count / 3);
+  const uint32_t nsub = (uint32_t)(count / per);
   const uint32_t nbatches = (nsub + SWR_BATCH_PRIMS - 1) / SWR_BATCH_PRIMS;
   const SwrTargetDesc T = make_target(c);
   const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
-  int rc = ensure_capacity(c, (uint32_t)nverts, vs->S, nsub, nbatches, ntiles, ps->R);
+  int rc = ensure_capacity(c, (uint32_t)nverts, vs->S, nsub, nbatches, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R);
   if (rc) return rc;
   SwrDrawDesc D;
   fill_draw(c, D, mode);
@@ -401,16 +472,20 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   aa.batch_counts = c->batch_counts.as<uint2>();
   aa.batch_base = c->batch_base.as<uint32_t>();
   aa.tris = c->tris.as<uint4>();
+  aa.lp_refs = c->lp_refs.as<uint2>();
   aa.status = st;
   aa.cap_clip_slots = c->cap_clip_slots;
   aa.cap_clip_verts = c->cap_clip_verts;
   aa.cap_prims = c->cap_prims;
-  vs->assemble_count(aa, nbatches, s);
+  if (mode == SWR_DRAW_TRIANGLE) vs->assemble_count(aa, nbatches, s);
+  else vs->assemble_lp_count(aa, nbatches, s);
   k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
                                   c->cap_prims);
-  vs->assemble_emit(aa, nbatches, s);
+  if (mode == SWR_DRAW_TRIANGLE) vs->assemble_emit(aa, nbatches, s);
+  else vs->assemble_lp_emit(aa, nbatches, s);
   mark(c, 2, s);
   c->last_ntiles = ntiles;
+  if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, T, s);
   return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s);
 }
 
@@ -419,14 +494,15 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   if (!c || !c->have_u) return SWR_EINVAL;
   const PsOps* ps = ps_ops(c->ps_id);
   if (!ps) return SWR_EINVAL;
-  if (mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;
-  if (count % 3 || count / 3 >= 0x7fffffffull || nverts >= 0x7fffffffull) return SWR_EINVAL;
+  if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
+  const int per = mode == SWR_DRAW_POINT ? 1 : (mode == SWR_DRAW_LINE ? 2 : 3);
+  if (count % per || count / per >= 0x7fffffffull || nverts >= 0x7fffffffull) return SWR_EINVAL;
   if ((count && !indices) || (nverts && !vertices)) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t nsub = (uint32_t)(count / 3);
+  const uint32_t nsub = (uint32_t)(count / per);
   const SwrTargetDesc T = make_target(c);
   const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
-  int rc = ensure_capacity(c, (uint32_t)nverts, ps->S, nsub, 1, ntiles, ps->R);
+  int rc = ensure_capacity(c, (uint32_t)nverts, ps->S, nsub, 1, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R);
   if (rc) return rc;
   if (!c->direct_keep.ensure((size_t)nsub * 4 + 16) || !c->direct_pos.ensure((size_t)nsub * 4 + 16))
     return SWR_ENOMEM;
@@ -443,14 +519,15 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   c->launches += (nverts ? 1 : 0) + (nsub ? 5 : 0);
   if (nsub) {
     const int grid = (int)((nsub + 255) / 256 < 1216 ? (nsub + 255) / 256 : 1216);
-    k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, 3, c->direct_keep.as<uint32_t>());
+    k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, per, c->direct_keep.as<uint32_t>());
     scan_exclusive(c->direct_keep.as<uint32_t>(), c->direct_pos.as<uint32_t>(), nullptr, nsub,
                    st + SWR_ST_PRIMS, c->scratch.as<uint32_t>(), s);
-    k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, 3, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
+    k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, per, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
                                        c->direct_pos.as<uint32_t>(), c->tris.as<uint4>(), st);
   }
   mark(c, 2, s);
   c->last_ntiles = ntiles;
+  if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, T, s);
   return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s);
 }
 

@@ -64,7 +64,8 @@ struct SwrTargetDesc {
   int32_t tiles_x, tiles_y;
   uint32_t tile_base;
   int32_t first_draw;  // draw whose uniforms carry the framebuffer pointers
-  int32_t _pad[2];
+  uint32_t pixel_base;  // first global pixel key of this target (point / line fragments)
+  int32_t _pad;
 };
 
 // Result of clipping one triangle (PolyClipper, PolyClipper.cpp:45-81): a polygon of up

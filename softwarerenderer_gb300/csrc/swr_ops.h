@@ -2,7 +2,7 @@
 // (VertexProcessor.h:77-85, Rasterizer.h:90-96).  Each built-in shader is compiled into
 // its own kernels; the context picks the launchers by program id.
 #pragma once
-#include "swr_stages.cuh"
+#include "swr_lines.cuh"
 
 namespace swr {
 
@@ -13,6 +13,8 @@ struct VsOps {
                  float* ptv, cudaStream_t s);
   void (*assemble_count)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
   void (*assemble_emit)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
+  void (*assemble_lp_count)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);  // points, lines
+  void (*assemble_lp_emit)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
 };
 
 struct PsOps {
@@ -24,6 +26,10 @@ struct PsOps {
                      uint32_t cap_pairs, const SwrDrawDesc* draws, const SwrTargetDesc* targets,
                      int tile, uint32_t* keys, uint32_t* vals, uint32_t* status_w, cudaStream_t s);
   void (*raster)(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s);
+  int lp_R;  // point / line record words
+  void (*lp_setup)(const SetupArgs& a, cudaStream_t s);
+  void (*lp_frags)(const LpFragArgs& a, cudaStream_t s);
+  void (*lp_shade)(const LpShadeArgs& a, cudaStream_t s);
 };
 
 const VsOps* vs_ops(int id);

@@ -37,6 +37,21 @@ void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) 
 }
 
 template <class PS>
+void run_lp_setup(const SetupArgs& a, cudaStream_t s) {
+  k_lp_setup<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+void run_lp_frags(const LpFragArgs& a, cudaStream_t s) {
+  k_lp_frags<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+void run_lp_shade(const LpShadeArgs& a, cudaStream_t s) {
+  k_lp_shade<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
 PsOps make() {
   PsOps o;
   o.A = PS::AVarCount;
@@ -47,6 +62,10 @@ PsOps make() {
   o.setup = &run_setup<PS>;
   o.emit_pairs = &run_pairs<PS>;
   o.raster = &run_raster<PS>;
+  o.lp_R = LpRec<PS>::R;
+  o.lp_setup = &run_lp_setup<PS>;
+  o.lp_frags = &run_lp_frags<PS>;
+  o.lp_shade = &run_lp_shade<PS>;
   return o;
 }
 

@@ -189,6 +189,7 @@ struct AssembleArgs {
   uint2* batch_counts;      // per batch: (kept input slots, kept extra fan triangles)
   const uint32_t* batch_base;
   uint4* tris;              // output primitives: v0, v1, v2 references + draw id
+  uint2* lp_refs;           // per submitted point / line: endpoint references after clipping
   uint32_t* status;
   uint32_t cap_clip_slots, cap_clip_verts, cap_prims;
 };

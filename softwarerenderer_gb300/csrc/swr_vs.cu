@@ -26,6 +26,15 @@ void run_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
 }
 
 template <class VS>
+void run_lp_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
+  if (nbatches) k_assemble_lp_count<VS::AVarCount, VS::PVarCount><<<nbatches, 256, 0, s>>>(a);
+}
+
+void run_lp_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
+  if (nbatches) k_assemble_lp_emit<<<nbatches, 256, 0, s>>>(a);
+}
+
+template <class VS>
 VsOps make() {
   VsOps o;
   o.attribs = VS::AttribCount;
@@ -37,6 +46,8 @@ VsOps make() {
   o.vertex = &run_vertex<VS>;
   o.assemble_count = &run_count<VS>;
   o.assemble_emit = &run_emit<VS>;
+  o.assemble_lp_count = &run_lp_count<VS>;
+  o.assemble_lp_emit = &run_lp_emit;
   return o;
 }
 

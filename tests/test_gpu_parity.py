@@ -69,3 +69,16 @@ def test_batch_boundary_clip_fans(gpu_lib, port):
     for seed in (7, 8):
         sc = scenes.random_scene(seed, direct=False, draw_mode=DrawMode.Triangle, n_prims=3000)
         _check(port, sc)
+
+
+@pytest.mark.parametrize("seed", range(0, 60))
+@pytest.mark.parametrize("mode", [DrawMode.Line, DrawMode.Point])
+def test_random_lines_points(gpu_lib, port, seed, mode):
+    sc = scenes.random_scene(2000 + seed, draw_mode=mode)
+    _check(port, sc)
+
+
+@pytest.mark.parametrize("mode", [DrawMode.Line, DrawMode.Point])
+def test_many_lines_points_multi_batch(gpu_lib, port, mode):
+    sc = scenes.random_scene(77, direct=False, draw_mode=mode, n_prims=2600)
+    _check(port, sc)
