@@ -233,7 +233,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   mark(c, 5, s);
   k_close_draw<<<1, 1, 0, s>>>(st);
   const int passes = (bits_for(ntiles) + 7) / 8;
-  c->launches += 1 + 3 + 1 + 5 * passes + 1 + (ntiles ? 1 : 0) + 1;
+  c->launches += 1 + 2 + 1 + 3 * passes + 1 + (ntiles ? 1 : 0) + 1;
   return cuda_err(cudaGetLastError());
 }
 
@@ -302,7 +302,7 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
   ps->lp_shade(sh, s);
   mark(c, 5, s);
   k_close_draw<<<1, 1, 0, s>>>(st);
-  c->launches += 1 + 3 + 1 + 5 * ((bits + 7) / 8) + 1 + 1;
+  c->launches += 1 + 2 + 1 + 3 * ((bits + 7) / 8) + 1 + 1;
   return cuda_err(cudaGetLastError());
 }
 
@@ -459,7 +459,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   mark(c, 0, s);
   vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts, c->ptv.as<float>(), s);
   mark(c, 1, s);
-  c->launches += (nverts ? 1 : 0) + (nbatches ? 2 : 0) + 1;
+  c->launches += (nverts ? 1 : 0) + (nbatches ? 2 : 0) + (mode == SWR_DRAW_TRIANGLE ? 0 : 1);
   AssembleArgs aa;
   aa.draws = c->draws.as<SwrDrawDesc>();
   aa.ndraws = 1;
@@ -477,12 +477,15 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   aa.cap_clip_slots = c->cap_clip_slots;
   aa.cap_clip_verts = c->cap_clip_verts;
   aa.cap_prims = c->cap_prims;
-  if (mode == SWR_DRAW_TRIANGLE) vs->assemble_count(aa, nbatches, s);
-  else vs->assemble_lp_count(aa, nbatches, s);
-  k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
-                                  c->cap_prims);
-  if (mode == SWR_DRAW_TRIANGLE) vs->assemble_emit(aa, nbatches, s);
-  else vs->assemble_lp_emit(aa, nbatches, s);
+  if (mode == SWR_DRAW_TRIANGLE) {
+    vs->assemble_count(aa, nbatches, s);
+    vs->assemble_emit(aa, nbatches, s);  // derives batch bases and the primitive count itself
+  } else {
+    vs->assemble_lp_count(aa, nbatches, s);
+    k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
+                                    c->cap_prims);
+    vs->assemble_lp_emit(aa, nbatches, s);
+  }
   mark(c, 2, s);
   c->last_ntiles = ntiles;
   if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, T, s);
@@ -516,7 +519,7 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   mark(c, 0, s);
   ps->direct_vertices(vertices, (uint32_t)nverts, c->ptv.as<float>(), s);
   mark(c, 1, s);
-  c->launches += (nverts ? 1 : 0) + (nsub ? 5 : 0);
+  c->launches += (nverts ? 1 : 0) + (nsub ? 4 : 0);
   if (nsub) {
     const int grid = (int)((nsub + 255) / 256 < 1216 ? (nsub + 255) / 256 : 1216);
     k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, per, c->direct_keep.as<uint32_t>());

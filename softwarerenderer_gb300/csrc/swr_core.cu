@@ -11,6 +11,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTile = 1024;  // items per block iteration (4 per thread)
+constexpr int kSortBlocks = 304;  // radix-sort blocks (2 per SM)
 
 __device__ __forceinline__ uint32_t load_n(const uint32_t* n_dev, uint32_t n_max) {
   if (!n_dev) return n_max;
@@ -39,23 +40,31 @@ __global__ void __launch_bounds__(kThreads) k_scan_reduce(const uint32_t* in, co
   if (threadIdx.x == 0) partials[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* partials, int nparts, uint32_t* total) {
-  __shared__ uint32_t tmp[32];
-  const uint32_t v = threadIdx.x < (unsigned)nparts ? partials[threadIdx.x] : 0u;
-  uint32_t tot;
-  const uint32_t ex = swr_block_exscan(v, tmp, &tot);
-  if (threadIdx.x < (unsigned)nparts) partials[threadIdx.x] = ex;
-  if (threadIdx.x == 0 && total) *total = tot;
-}
-
 __global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* in, uint32_t* out,
                                                         const uint32_t* n_dev, uint32_t n_max,
-                                                        uint32_t chunk, const uint32_t* partials) {
+                                                        uint32_t chunk, const uint32_t* partials,
+                                                        uint32_t* total) {
   __shared__ uint32_t tmp[32];
   const uint32_t n = load_n(n_dev, n_max);
   uint32_t b, e;
   chunk_range(n, chunk, b, e);
-  uint32_t run = partials[blockIdx.x];
+  // prefix of the partial sums of the blocks before this one (and the grand total)
+  __shared__ uint32_t pref[2];
+  {
+    uint32_t mine = 0, all = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) {
+      const uint32_t v = partials[i];
+      all += v;
+      if (i < (int)blockIdx.x) mine += v;
+    }
+    uint32_t t0, t1;
+    swr_block_exscan(mine, tmp, &t0);
+    swr_block_exscan(all, tmp, &t1);
+    if (threadIdx.x == 0) { pref[0] = t0; pref[1] = t1; }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && total) *total = pref[1];
+  uint32_t run = pref[0];
   for (uint32_t base = b; base < e; base += kTile) {
     uint32_t v[4], s = 0;
 #pragma unroll
@@ -97,7 +106,28 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(const uint32_t* keys, c
   chunk_range(n, chunk, b, e);
   for (uint32_t i = b + threadIdx.x; i < e; i += kThreads) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
   __syncthreads();
-  hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+  hist[blockIdx.x * 256 + threadIdx.x] = cnt[threadIdx.x];  // [block][digit]
+}
+
+// Per-digit exclusive prefix over the block histograms, one warp per digit:
+// off[b][d] = digit-d keys in blocks before b; tot[d] = all digit-d keys.
+__global__ void __launch_bounds__(256) k_radix_offsets(const uint32_t* hist, uint32_t* off, uint32_t* tot,
+                                                       int nblocks) {
+  const int d = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  uint32_t run = 0;
+  for (int b0 = 0; b0 < nblocks; b0 += 32) {
+    const int b = b0 + lane;
+    const uint32_t v = b < nblocks ? hist[b * 256 + d] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (b < nblocks) off[b * 256 + d] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+  if (lane == 0) tot[d] = run;
 }
 
 // Stable scatter: the block walks its chunk in 1024-item tiles; warp w ranks items
@@ -107,13 +137,18 @@ __global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* kin,
                                                             uint32_t* kout, uint32_t* vout,
                                                             const uint32_t* n_dev, uint32_t n_max,
                                                             uint32_t chunk, int shift,
-                                                            const uint32_t* hist_ex, int nblocks) {
+                                                            const uint32_t* off, const uint32_t* tot) {
   __shared__ uint32_t wcnt[kWarps][256];
   __shared__ uint32_t base[256];
   __shared__ uint32_t tile_tot[256];
+  __shared__ uint32_t tmp[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
-  base[threadIdx.x] = hist_ex[threadIdx.x * nblocks + blockIdx.x];
+  {
+    // digit d starts at (keys with a smaller digit) + (digit-d keys in earlier blocks)
+    const uint32_t dbase = swr_block_exscan(tot[threadIdx.x], tmp, nullptr);
+    base[threadIdx.x] = dbase + off[blockIdx.x * 256 + threadIdx.x];
+  }
   __syncthreads();
   const uint32_t n = load_n(n_dev, n_max);
   uint32_t b, e;
@@ -181,28 +216,26 @@ void scan_exclusive(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, ui
                     uint32_t* total, uint32_t* scratch, cudaStream_t s) {
   const uint32_t chunk = chunk_for(n_max, kScanBlocks);
   k_scan_reduce<<<kScanBlocks, kThreads, 0, s>>>(in, n_dev, n_max, chunk, scratch);
-  k_scan_partials<<<1, 1024, 0, s>>>(scratch, kScanBlocks, total);
-  k_scan_down<<<kScanBlocks, kThreads, 0, s>>>(in, out, n_dev, n_max, chunk, scratch);
+  k_scan_down<<<kScanBlocks, kThreads, 0, s>>>(in, out, n_dev, n_max, chunk, scratch, total);
 }
 
-size_t sort_scratch_words(uint32_t) { return 2 * 256 * kScanBlocks + scan_scratch_words(256 * kScanBlocks); }
+size_t sort_scratch_words(uint32_t) { return 2 * 256 * kSortBlocks + 256; }
 
 int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, const uint32_t* n_dev,
                      uint32_t n_max, int bits, uint32_t* scratch, cudaStream_t s) {
-  const uint32_t chunk = chunk_for(n_max, kScanBlocks);
+  const uint32_t chunk = chunk_for(n_max, kSortBlocks);
   uint32_t* hist = scratch;
-  uint32_t* hist_ex = scratch + 256 * kScanBlocks;
-  uint32_t* scan_tmp = scratch + 2 * 256 * kScanBlocks;
+  uint32_t* off = scratch + 256 * kSortBlocks;
+  uint32_t* tot = scratch + 2 * 256 * kSortBlocks;
   int cur = 0;
   for (int shift = 0; shift < bits; shift += 8) {
     uint32_t* ki = cur ? k1 : k0;
     uint32_t* vi = cur ? v1 : v0;
     uint32_t* ko = cur ? k0 : k1;
     uint32_t* vo = cur ? v0 : v1;
-    k_radix_hist<<<kScanBlocks, kThreads, 0, s>>>(ki, n_dev, n_max, chunk, shift, hist, kScanBlocks);
-    scan_exclusive(hist, hist_ex, nullptr, 256 * kScanBlocks, nullptr, scan_tmp, s);
-    k_radix_scatter<<<kScanBlocks, kThreads, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, chunk, shift,
-                                                     hist_ex, kScanBlocks);
+    k_radix_hist<<<kSortBlocks, kThreads, 0, s>>>(ki, n_dev, n_max, chunk, shift, hist, kSortBlocks);
+    k_radix_offsets<<<32, 256, 0, s>>>(hist, off, tot, kSortBlocks);
+    k_radix_scatter<<<kSortBlocks, kThreads, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, chunk, shift, off, tot);
     cur ^= 1;
   }
   return cur;
@@ -210,7 +243,9 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, con
 
 void segment_starts(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max, uint32_t ntiles,
                     uint32_t* start, cudaStream_t s) {
-  k_segment_starts<<<2 * 152, 256, 0, s>>>(keys, n_dev, n_max, ntiles, start);
+  const uint32_t want = (n_max + 1 + 255) / 256;
+  const int grid = (int)(want < 8192u ? want : 8192u);
+  k_segment_starts<<<grid, 256, 0, s>>>(keys, n_dev, n_max, ntiles, start);
 }
 
 }  // namespace swr

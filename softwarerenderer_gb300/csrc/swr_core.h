@@ -12,12 +12,14 @@ constexpr int kScanBlocks = 304;  // 2 x 152 SMs
 
 // Exclusive prefix sum of in[0..n) into out, where n = min(*n_dev, n_max) when n_dev is
 // given (device-resident length) else n_max.  total (device) receives the sum.
-// scratch needs scan_scratch_words(n_max) words.
+// scratch needs scan_scratch_words(n_max) words.  Two kernels: block partial sums, then
+// each block prefixes the partials before it and scans its chunk.
 size_t scan_scratch_words(uint32_t n_max);
 void scan_exclusive(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_max,
                     uint32_t* total, uint32_t* scratch, cudaStream_t s);
 
-// Stable LSD radix sort of (key, value) pairs by the low `bits` bits of key.
+// Stable LSD radix sort of (key, value) pairs by the low `bits` bits of key; three kernels
+// per 8-bit pass (block histograms, per-digit offsets, stable scatter).
 // n = min(*n_dev, n_max).  Ping-pongs between (k0,v0) and (k1,v1); returns 0 when the
 // result ends in (k0, v0), 1 when it ends in (k1, v1).  scratch: sort_scratch_words(n_max).
 size_t sort_scratch_words(uint32_t n_max);

@@ -14,9 +14,12 @@
 // Pixel shader contract: static AVarCount, PVarCount, InterpolateZ, InterpolateW
 // (PixelShaderBase.h:44-53), a per-pixel State that the reference keeps in the
 // shader's own static buffers (with `frags` and `writes` counters), and
-// load / drawPixel / store / earlyReject.  earlyReject(z, s) returns true when
-// drawPixel with depth z would do nothing but count the fragment (a failing depth test);
-// it then counts it itself, so the rasterizer may skip building the other interpolants.  drawPixel is the
+// load / drawPixel / store / earlyReject / shade / apply.  earlyReject(z, s) returns true
+// when drawPixel with depth z would do nothing but count the fragment (a failing depth
+// test); it then counts it itself, so the rasterizer may skip building the other
+// interpolants.  Every built-in drawPixel is apply(s, z, shade(p, u), prim) with shade a
+// pure function of the fragment and the uniforms (evaluated only when it is used), so the
+// rasterizer may compute shade() for a fragment early and apply() it in primitive order.  drawPixel is the
 // reference's drawPixel(const PixelData&) (PixelShaderBase.h:116); load/store move
 // the pixel's framebuffer values between memory and State.  Calling
 // load + drawPixel + store per fragment is exactly the reference's side effect; the
@@ -172,6 +175,19 @@ SWR_HD bool swr_depth_reject(float z, State& s) {
   return true;
 }
 
+// Colour write of the RGBA8 depth-tested shaders, and their drawPixel in apply() form.
+SWR_HD void swr_write(SwrStateRGBA8& s, float z, uint32_t c, int prim) {
+  s.depth = z;
+  s.color = c;
+  s.winner = prim;
+  s.writes++;
+}
+
+SWR_HD void swr_apply_depth(SwrStateRGBA8& s, float z, uint32_t c, int prim) {
+  s.frags++;
+  if (z < s.depth) swr_write(s, z, c, prim);
+}
+
 template <bool kDepth>
 SWR_HD void swr_load_rgba8(SwrStateRGBA8& s, int x, int y, const SwrUniforms& u) {
   const size_t i = (size_t)y * (size_t)u.width + (size_t)x;
@@ -209,15 +225,16 @@ struct PsTexNearest {
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
   SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
+  typedef uint32_t Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms& u) {
+    return swr_tex_nearest(u, p.pvar[0], p.pvar[1]) | 0xff000000u;
+  }
+  SWR_HD static void apply(State& s, float z, Color c, int prim) { swr_apply_depth(s, z, c, prim); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
-    if (p.z < s.depth) {
-      s.depth = p.z;
-      s.color = swr_tex_nearest(u, p.pvar[0], p.pvar[1]) | 0xff000000u;
-      s.winner = prim;
-      s.writes++;
-    }
+    if (p.z < s.depth) swr_write(s, p.z, shade(p, u), prim);
   }
 };
 
@@ -244,18 +261,19 @@ struct PsLambert {
     const int cv = swr_trunc_int(swr_mul(swr_clamp01(tv), (float)u.checker));
     return ((cu + cv) & 1) ? 1.0f : 0.55f;
   }
+  typedef uint32_t Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms& u) {
+    const float li = intensity(p.avar[0], p.avar[1], p.avar[2], u);
+    const float al = checker(p.pvar[0], p.pvar[1], u);
+    const float c = swr_mul(al, li);
+    return swr_pack_rgba8(c, swr_mul(c, 0.9f), swr_mul(c, 0.75f), 1.0f);
+  }
+  SWR_HD static void apply(State& s, float z, Color c, int prim) { swr_apply_depth(s, z, c, prim); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
-    if (p.z < s.depth) {
-      const float li = intensity(p.avar[0], p.avar[1], p.avar[2], u);
-      const float al = checker(p.pvar[0], p.pvar[1], u);
-      const float c = swr_mul(al, li);
-      s.depth = p.z;
-      s.color = swr_pack_rgba8(c, swr_mul(c, 0.9f), swr_mul(c, 0.75f), 1.0f);
-      s.winner = prim;
-      s.writes++;
-    }
+    if (p.z < s.depth) swr_write(s, p.z, shade(p, u), prim);
   }
 };
 
@@ -266,19 +284,20 @@ struct PsLambertTex {
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
   SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
+  typedef uint32_t Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms& u) {
+    const float li = PsLambert::intensity(p.avar[0], p.avar[1], p.avar[2], u);
+    const uint32_t t = swr_tex_nearest(u, p.pvar[0], p.pvar[1]);
+    const float sc = swr_div(li, 255.0f);
+    return swr_pack_rgba8(swr_mul(swr_u8_channel(t, 0), sc), swr_mul(swr_u8_channel(t, 8), sc),
+                          swr_mul(swr_u8_channel(t, 16), sc), 1.0f);
+  }
+  SWR_HD static void apply(State& s, float z, Color c, int prim) { swr_apply_depth(s, z, c, prim); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
-    if (p.z < s.depth) {
-      const float li = PsLambert::intensity(p.avar[0], p.avar[1], p.avar[2], u);
-      const uint32_t t = swr_tex_nearest(u, p.pvar[0], p.pvar[1]);
-      const float sc = swr_div(li, 255.0f);
-      s.depth = p.z;
-      s.color = swr_pack_rgba8(swr_mul(swr_u8_channel(t, 0), sc), swr_mul(swr_u8_channel(t, 8), sc),
-                               swr_mul(swr_u8_channel(t, 16), sc), 1.0f);
-      s.winner = prim;
-      s.writes++;
-    }
+    if (p.z < s.depth) swr_write(s, p.z, shade(p, u), prim);
   }
 };
 
@@ -289,15 +308,16 @@ struct PsVColor {
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
   SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
+  typedef uint32_t Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms&) {
+    return swr_pack_rgba8(p.pvar[0], p.pvar[1], p.pvar[2], 1.0f);
+  }
+  SWR_HD static void apply(State& s, float z, Color c, int prim) { swr_apply_depth(s, z, c, prim); }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
-    if (p.z < s.depth) {
-      s.depth = p.z;
-      s.color = swr_pack_rgba8(p.pvar[0], p.pvar[1], p.pvar[2], 1.0f);
-      s.winner = prim;
-      s.writes++;
-    }
+    if (p.z < s.depth) swr_write(s, p.z, shade(p, u), prim);
   }
 };
 
@@ -310,12 +330,20 @@ struct PsVColorAffine {
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<false>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, false); }
   SWR_HD static bool earlyReject(float, State&) { return false; }
+  typedef uint32_t Color;
   template <class PD>
-  SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
+  SWR_HD static Color shade(const PD& p, const SwrUniforms&) {
+    return swr_pack_rgba8(p.avar[0], p.avar[1], p.avar[2], 1.0f);
+  }
+  SWR_HD static void apply(State& s, float, Color c, int prim) {
     s.frags++;
-    s.color = swr_pack_rgba8(p.avar[0], p.avar[1], p.avar[2], 1.0f);
+    s.color = c;
     s.winner = prim;
     s.writes++;
+  }
+  template <class PD>
+  SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
+    apply(s, 0.0f, shade(p, u), prim);
   }
 };
 
@@ -368,20 +396,34 @@ struct PsDiff {
     }
     if (u.frag_count && s.frags) u.frag_count[i] += s.frags;
   }
+  struct Color {
+    float c[4];
+  };
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms& u) {
+    float t[4];
+    swr_tex_bilinear_f32(u, p.pvar[3], p.pvar[4], t);
+    Color o;
+    o.c[0] = swr_mul(p.pvar[0], t[0]);
+    o.c[1] = swr_mul(p.pvar[1], t[1]);
+    o.c[2] = swr_mul(p.pvar[2], t[2]);
+    o.c[3] = t[3];
+    return o;
+  }
+  SWR_HD static void write(State& s, float z, const Color& c, int prim) {
+    s.depth = z;
+    s.color[0] = c.c[0]; s.color[1] = c.c[1]; s.color[2] = c.c[2]; s.color[3] = c.c[3];
+    s.winner = prim;
+    s.writes++;
+  }
+  SWR_HD static void apply(State& s, float z, const Color& c, int prim) {
+    s.frags++;
+    if (z < s.depth) write(s, z, c, prim);
+  }
   template <class PD>
   SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
     s.frags++;
-    if (p.z < s.depth) {
-      float t[4];
-      swr_tex_bilinear_f32(u, p.pvar[3], p.pvar[4], t);
-      s.depth = p.z;
-      s.color[0] = swr_mul(p.pvar[0], t[0]);
-      s.color[1] = swr_mul(p.pvar[1], t[1]);
-      s.color[2] = swr_mul(p.pvar[2], t[2]);
-      s.color[3] = t[3];
-      s.winner = prim;
-      s.writes++;
-    }
+    if (p.z < s.depth) write(s, p.z, shade(p, u), prim);
   }
 };
 

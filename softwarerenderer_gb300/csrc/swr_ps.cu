@@ -17,7 +17,7 @@ void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {
 
 template <class PS>
 void run_setup(const SetupArgs& a, cudaStream_t s) {
-  k_setup<PS><<<kGrid, 256, 0, s>>>(a);
+  k_setup<PS><<<kGrid, kSetupThreads, 0, s>>>(a);
 }
 
 template <class PS>

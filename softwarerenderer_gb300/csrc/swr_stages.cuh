@@ -195,12 +195,11 @@ struct AssembleArgs {
 };
 
 template <int A, int P>
-__device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, int d, uint32_t p,
-                             uint32_t& in_kept, uint32_t& ex_kept) {
+__device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, uint32_t p, uint32_t i0,
+                             uint32_t i1, uint32_t i2, uint32_t& in_kept, uint32_t& ex_kept) {
   typedef VLayout<A, P> L;
   in_kept = ex_kept = 0;
   const uint32_t gp = D.pbase + p;
-  const uint32_t i0 = D.indices[3 * p], i1 = D.indices[3 * p + 1], i2 = D.indices[3 * p + 2];
   if (i0 >= D.nverts || i1 >= D.nverts || i2 >= D.nverts) {
     atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_BAD_INDEX);
     g.tri_flags[gp] = 0;
@@ -290,27 +289,38 @@ __device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, int d,
   ex_kept = __popc(keep >> 1);
 }
 
+// The batch's 3 x 1024 indices, loaded cooperatively (coalesced) into shared memory.
+__device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uint32_t p0, uint32_t* sidx) {
+  const uint32_t n = min((uint32_t)SWR_BATCH_PRIMS, D.nprims - p0);
+  const uint32_t* src = D.indices + (size_t)3 * p0;
+  for (uint32_t i = threadIdx.x; i < 3 * n; i += blockDim.x) sidx[i] = src[i];
+  __syncthreads();
+  return n;
+}
+
 template <int A, int P>
 __global__ void __launch_bounds__(256) k_assemble_count(AssembleArgs g) {
   __shared__ uint32_t tmp[32];
+  __shared__ uint32_t sidx[3 * SWR_BATCH_PRIMS];
   const uint32_t b = blockIdx.x;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
+  const uint32_t n = load_batch_indices(D, p0, sidx);
+  // four triangles per thread, strided so a warp's triangles are consecutive
   uint32_t in_sum = 0, ex_sum = 0;
   for (int j = 0; j < 4; ++j) {
-    const uint32_t p = p0 + threadIdx.x * 4 + j;
-    if (p < D.nprims && p < p0 + SWR_BATCH_PRIMS) {
+    const uint32_t q = j * 256 + threadIdx.x;
+    if (q < n) {
       uint32_t ik, ek;
-      assemble_one<A, P>(g, D, d, p, ik, ek);
+      assemble_one<A, P>(g, D, p0 + q, sidx[3 * q], sidx[3 * q + 1], sidx[3 * q + 2], ik, ek);
       in_sum += ik;
       ex_sum += ek;
     }
   }
-  const uint32_t packed_in = in_sum, packed_ex = ex_sum;
   uint32_t tin, tex;
-  swr_block_exscan(packed_in, tmp, &tin);
-  swr_block_exscan(packed_ex, tmp, &tex);
+  swr_block_exscan(in_sum, tmp, &tin);
+  swr_block_exscan(ex_sum, tmp, &tex);
   if (threadIdx.x == 0) g.batch_counts[b] = make_uint2(tin, tex);
 }
 
@@ -333,59 +343,63 @@ static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts,
   }
 }
 
+// Writes the surviving triangles of one batch at their effective-order positions.  The
+// batch base is the sum of the totals of the batches before it; the last batch publishes
+// the primitive count (and flags an undersized primitive queue).
 template <int A, int P>
-__global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
+__global__ void __launch_bounds__(SWR_BATCH_PRIMS) k_assemble_emit(AssembleArgs g) {
   __shared__ uint32_t tmp[32];
+  __shared__ uint32_t sidx[3 * SWR_BATCH_PRIMS];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t b = blockIdx.x;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
-  uint32_t fl[4], slot[4], in_sum = 0, ex_sum = 0;
-  uint16_t keep[4];
-  for (int j = 0; j < 4; ++j) {
-    const uint32_t p = p0 + threadIdx.x * 4 + j;
-    fl[j] = 0;
-    keep[j] = 0;
-    slot[j] = 0xffffffffu;
-    if (p < D.nprims && p < p0 + SWR_BATCH_PRIMS) {
-      fl[j] = g.tri_flags[D.pbase + p];
-      if (fl[j] & 4) {
-        slot[j] = g.clip_slot[D.pbase + p];
-        if (slot[j] != 0xffffffffu) keep[j] = g.clip_table[slot[j]].keep;
-      } else {
-        keep[j] = fl[j] & 1;
-      }
-      in_sum += keep[j] & 1;
-      ex_sum += __popc(keep[j] >> 1);
+  const uint32_t n = load_batch_indices(D, p0, sidx);
+  uint32_t before = 0;
+  for (uint32_t i = threadIdx.x; i < b; i += blockDim.x) before += g.batch_counts[i].x + g.batch_counts[i].y;
+  uint32_t base;
+  swr_block_exscan(before, tmp, &base);
+  const uint32_t q = threadIdx.x;
+  uint32_t fl = 0, slot = 0xffffffffu;
+  uint32_t keep = 0;
+  if (q < n) {
+    fl = g.tri_flags[D.pbase + p0 + q];
+    if (fl & 4) {
+      slot = g.clip_slot[D.pbase + p0 + q];
+      if (slot != 0xffffffffu) keep = g.clip_table[slot].keep;
+    } else {
+      keep = fl & 1;
     }
   }
   uint32_t tin, tex;
-  uint32_t rin = swr_block_exscan(in_sum, tmp, &tin);
-  uint32_t rex = swr_block_exscan(ex_sum, tmp, &tex);
-  const uint32_t base = g.batch_base[b];
-  for (int j = 0; j < 4; ++j) {
-    const uint32_t p = p0 + threadIdx.x * 4 + j;
-    if (!keep[j]) continue;
-    if (!(fl[j] & 4)) {
-      uint32_t r0 = D.vbase + D.indices[3 * p], r1 = D.vbase + D.indices[3 * p + 1],
-               r2 = D.vbase + D.indices[3 * p + 2];
-      if (fl[j] & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
-      g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
-      rin++;
-    } else {
-      const SwrClipEntry e = g.clip_table[slot[j]];
-      for (int k = 0; k + 2 < e.n; ++k) {
-        if (!((e.keep >> k) & 1)) continue;
-        uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
-        if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
-        if (k == 0) {
-          g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
-          rin++;
-        } else {
-          g.tris[base + tin + rex] = make_uint4(r0, r1, r2, (uint32_t)d);
-          rex++;
-        }
+  uint32_t rin = swr_block_exscan(keep & 1u, tmp, &tin);
+  uint32_t rex = swr_block_exscan(__popc(keep >> 1), tmp, &tex);
+  if (b == gridDim.x - 1 && threadIdx.x == 0) {
+    g.status[SWR_ST_PRIMS] = base + tin + tex;
+    if (base + tin + tex > g.cap_prims) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
+  }
+  if (base + tin + tex > g.cap_prims) {
+    if (threadIdx.x == 0) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
+    return;
+  }
+  if (!keep) return;
+  if (!(fl & 4)) {
+    uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
+    if (fl & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
+    g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
+  } else {
+    // first fan triangle in the input slot, the others after all of the batch's slots
+    const SwrClipEntry e = g.clip_table[slot];
+    for (int k = 0; k + 2 < e.n; ++k) {
+      if (!((e.keep >> k) & 1)) continue;
+      uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
+      if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
+      if (k == 0) {
+        g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
+      } else {
+        g.tris[base + tin + rex] = make_uint4(r0, r1, r2, (uint32_t)d);
+        rex++;
       }
     }
   }
@@ -498,13 +512,21 @@ __device__ __forceinline__ void span_row(const SpanHalf& h, int y, int minx, int
   xr = swr_mini(maxx, swr_trunc_int(c2));
 }
 
+// Records are assembled in shared memory and written out as contiguous float4 runs
+// (one record per thread would be a 4-byte store per 160-byte stride).
+constexpr int kSetupThreads = 128;
+
 template <class PS>
-__global__ void __launch_bounds__(256) k_setup(SetupArgs g) {
+__global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
   typedef Rec<PS> RL;
+  __shared__ float4 stage4[kSetupThreads * RL::R / 4];
+  float* stage = (float*)stage4;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   uint32_t np = g.status[SWR_ST_PRIMS];
   if (np > g.cap_prims) np = g.cap_prims;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+  for (uint32_t p0 = blockIdx.x * kSetupThreads; p0 < np; p0 += gridDim.x * kSetupThreads) {
+  const uint32_t p = p0 + threadIdx.x;
+  if (p < np) {
     const uint4 t = g.tris[p];
     const SwrDrawDesc& D = g.draws[t.w];
     const SwrTargetDesc& T = g.targets[D.target];
@@ -515,7 +537,7 @@ __global__ void __launch_bounds__(256) k_setup(SetupArgs g) {
       vp[k] = (rr[k] & SWR_CLIP_REF) ? g.clipv + (size_t)(rr[k] & ~SWR_CLIP_REF) * g.S : g.ptv + (size_t)rr[k] * g.S;
       x[k] = vp[k][4]; y[k] = vp[k][5]; z[k] = vp[k][6]; w[k] = vp[k][3];
     }
-    float* rec = g.recs + (size_t)p * RL::R;
+    float* rec = stage + threadIdx.x * RL::R;
     uint32_t tiles = 0;
     // TriangleEquations: e0 = (v1, v2), e1 = (v2, v0), e2 = (v0, v1)
     const Edge e0 = make_edge(x[1], y[1], x[2], y[2]);
@@ -671,6 +693,12 @@ __global__ void __launch_bounds__(256) k_setup(SetupArgs g) {
     rec[4] = __int_as_float(bx1); rec[5] = __int_as_float(by1);
     g.tile_count[p] = flags ? tiles : 0u;
   }
+  __syncthreads();
+  const uint32_t cnt = min((uint32_t)kSetupThreads, np - p0);
+  float4* dst = (float4*)(g.recs + (size_t)p0 * RL::R);
+  for (uint32_t i = threadIdx.x; i < cnt * (RL::R / 4); i += kSetupThreads) dst[i] = stage4[i];
+  __syncthreads();
+  }
 }
 
 // (tile, primitive) pairs in primitive order.
@@ -789,25 +817,89 @@ __device__ __forceinline__ uint64_t block_mask(const float* r, int flags, int bx
   return m;
 }
 
+// Position (0-63) of the j-th set bit of m (j < popcount(m)).
+__device__ __forceinline__ int nth_bit64(uint64_t m, int j) {
+  int off = 0;
+  uint32_t w = (uint32_t)m;
+  int c = __popc(w);
+  if (j >= c) { j -= c; w = (uint32_t)(m >> 32); off = 32; }
+  c = __popc(w & 0xffffu); if (j >= c) { j -= c; w >>= 16; off += 16; }
+  c = __popc(w & 0xffu);   if (j >= c) { j -= c; w >>= 8; off += 8; }
+  c = __popc(w & 0xfu);    if (j >= c) { j -= c; w >>= 4; off += 4; }
+  c = __popc(w & 0x3u);    if (j >= c) { j -= c; w >>= 2; off += 2; }
+  if (j >= (int)(w & 1u)) off += 1;
+  return off;
+}
+
+// Rebuilds the reference's incrementally stepped PixelData for pixel (x, y): the value
+// at the evaluation point (block corner or span start) stepped kb times along y and ka
+// times along x (PixelData::init/stepY/stepX, PixelData.h:61-125).
+template <class PS>
+__device__ __forceinline__ void build_pixel(const float* eq, bool blockmode, float fx, float fy, int ka, int kb,
+                                            GpuPixel<PS>& pd) {
+  typedef Rec<PS> RL;
+  if (RL::IW) {
+    const float* q3 = eq + 3 * RL::EQ_W;
+    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+    pd.invw = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
+    pd.w = swr_div(1.0f, pd.invw);
+  }
+#pragma unroll
+  for (int i = 0; i < RL::NA; ++i) {
+    const float* q3 = eq + 3 * (RL::EQ_A + i);
+    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+    pd.avar[i] = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
+  }
+#pragma unroll
+  for (int i = 0; i < RL::NP; ++i) {
+    const float* q3 = eq + 3 * (RL::EQ_P + i);
+    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+    const float pt = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
+    pd.pvar[i] = swr_mul(pt, pd.w);
+  }
+}
+
+template <class PS>
+__device__ __forceinline__ float build_z(const float* eq, bool blockmode, float fx, float fy, int ka, int kb) {
+  typedef Rec<PS> RL;
+  if (!RL::IZ) return 0.0f;
+  const float* q3 = eq + 3 * RL::EQ_Z;
+  const float z0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
+  return blockmode ? fold7(z0, q3[0], ka) : swr_fold(z0, q3[0], ka);
+}
+
 // One CTA per screen tile, 256 threads.  Per chunk of CH primitives of the tile's bin:
 //   A. stage the setup records in shared memory;
-//   B. one thread per (primitive, 8x8 block) computes the block's exact coverage mask and
-//      one thread per (primitive, tile row) the row's span ends [xl, xr);
-//   C. each thread walks the chunk in primitive order for the pixels it owns, tests
-//      coverage with one bit / one range, rebuilds the incrementally stepped interpolants
-//      of covered pixels (z first: a failing depth test needs nothing else) and calls the
-//      pixel shader on the pixel's register-resident State.
+//   B. one thread per (primitive, 8x8 block) computes the exact coverage mask: Block mode
+//      by the reference's corner classification and stepped edge tests, Span mode from the
+//      rows' [xl, xr) (also kept as the interpolation start of each row);
+//   C1. small primitives (<= 64 covered pixels in the tile, up to FB fragments per chunk)
+//      are compacted: one thread per covered fragment rebuilds the stepped interpolants and
+//      evaluates the pixel shader's pure shade() at full SIMT width;
+//   C2. each thread walks the chunk in primitive order for the pixels it owns and applies
+//      every covering fragment to the pixel's register-resident State: compacted fragments
+//      through apply(), others by rebuilding the interpolants in place (z first: a failing
+//      depth test needs nothing else) and drawPixel().
 template <class PS, int TILE, int CH>
-__global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
+__global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
   typedef Rec<PS> RL;
+  typedef typename PS::Color Color;
   constexpr int PPT = TILE * TILE / 256;  // pixels per thread
   constexpr int NBX = TILE / SWR_BLOCK;   // blocks per tile row
   constexpr int NB = NBX * NBX;
-  __shared__ float srec[CH * RL::R];
+  constexpr int FB = sizeof(Color) > 4 ? 512 : 1024;  // compacted fragments per chunk
+  constexpr int SMALL = 64;
+  __shared__ float4 srec4[CH * RL::R / 4];
+  float* srec = (float*)srec4;
   __shared__ uint64_t smask[CH * NB];
   __shared__ int2 sspan[CH * TILE];
   __shared__ uint32_t sids[CH];
+  __shared__ uint32_t sex[CH];   // compacted-fragment base (monotone over the chunk)
+  __shared__ uint8_t scomp[CH];  // 1: compacted
+  __shared__ float sfz[FB];
+  __shared__ Color sfc[FB];
   __shared__ uint32_t sfr[32];
+  __shared__ uint32_t snc;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t tile = blockIdx.x;
   const uint32_t b = g.tile_start[tile], e = g.tile_start[tile + 1];
@@ -839,106 +931,166 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs g) {
     const int n = (int)min((uint32_t)CH, e - c0);
     __syncthreads();
     if (threadIdx.x < n) sids[threadIdx.x] = g.bin[c0 + threadIdx.x];
+    if (threadIdx.x == 0) snc = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < n * RL::R; i += 256) {
-      const int k = i / RL::R, w = i - k * RL::R;
-      srec[i] = g.recs[(size_t)sids[k] * RL::R + w];
+    {
+      constexpr int R4 = RL::R / 4;
+      const float4* recs4 = (const float4*)g.recs;
+#pragma unroll 4
+      for (int i = threadIdx.x; i < n * R4; i += 256) {
+        const int k = i / R4, w = i - k * R4;
+        srec4[i] = recs4[(size_t)sids[k] * R4 + w];
+      }
     }
     __syncthreads();
-    // B: coverage per (primitive, block) and per (primitive, row)
+    // B: coverage per (primitive, block)
     for (int i = threadIdx.x; i < n * NB; i += 256) {
       const int k = i / NB, j = i - k * NB;
       const float* r = srec + k * RL::R;
       const int flags = __float_as_int(r[0]);
       const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
       uint64_t m = 0;
-      if ((flags & 3) == 3 && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
-          by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]))
-        m = block_mask(r, flags, bx, by);
-      smask[i] = m;
-    }
-    for (int i = threadIdx.x; i < n * TILE; i += 256) {
-      const int k = i / TILE, row = i - k * TILE;
-      const float* r = srec + k * RL::R;
-      const int flags = __float_as_int(r[0]);
-      const int y = oy + row;
-      int2 sp = make_int2(1, 0);
-      if ((flags & 3) == 1 && y >= __float_as_int(r[3]) && y <= __float_as_int(r[5])) {
-        SpanHalf h;
-        bool any = true;
-        if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
-          h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
-        } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
-          h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
-        } else {
-          any = false;
-        }
-        if (any) {
-          const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
-          span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
+      const bool hit = (flags & 1) && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
+                       by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]);
+      if (flags & 2) {
+        if (hit) m = block_mask(r, flags, bx, by);
+      } else if (flags & 1) {
+        const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+        for (int rr = 0; rr < SWR_BLOCK; ++rr) {
+          const int y = by + rr;
+          // the row's span does not depend on this block's x-overlap: the column-0 task
+          // stores it for every block of the row
+          int2 sp = make_int2(1, 0);
+          if (y >= __float_as_int(r[3]) && y <= __float_as_int(r[5])) {
+            SpanHalf h;
+            bool any = true;
+            if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
+              h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
+            } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
+              h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
+            } else {
+              any = false;
+            }
+            if (any) span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
+          }
+          if ((j % NBX) == 0) sspan[k * TILE + (y - oy)] = sp;
+          const int c0b = max(sp.x, bx) - bx, c1b = min(sp.y, bx + SWR_BLOCK) - bx;
+          if (hit && c1b > c0b) m |= (((1ull << (c1b - c0b)) - 1ull) << c0b) << (rr * 8);
         }
       }
-      sspan[i] = sp;
+      smask[i] = m;
     }
     __syncthreads();
-    // C: fragments in primitive order
+    // C1 set-up: compact the small primitives' fragments (a prefix of the chunk's small
+    // primitives whose fragments fit in FB)
+    {
+      uint32_t cnt = 0;
+      if (threadIdx.x < n) {
+        const float* r = srec + threadIdx.x * RL::R;
+        if (__float_as_int(r[0]) & 1)
+          for (int j = 0; j < NB; ++j) cnt += __popc((uint32_t)smask[threadIdx.x * NB + j]) +
+                                              __popc((uint32_t)(smask[threadIdx.x * NB + j] >> 32));
+      }
+      const uint32_t cand = cnt <= SMALL ? cnt : 0u;
+      uint32_t tot;
+      const uint32_t ex = swr_block_exscan(cand, sfr, &tot);
+      if (threadIdx.x < n) {
+        const bool comp = cnt <= SMALL && ex + cnt <= FB;
+        sex[threadIdx.x] = ex;
+        scomp[threadIdx.x] = comp ? 1 : 0;
+        if (comp && cnt) atomicMax(&snc, ex + cnt);
+      }
+      __syncthreads();
+    }
+    // C1: interpolate and shade the compacted fragments
+    const int nc = (int)snc;
+    for (int f = threadIdx.x; f < nc; f += 256) {
+      int lo = 0, hi = n - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((int)sex[mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      const int k = lo;
+      int jj = f - (int)sex[k];
+      const uint64_t* mk = smask + k * NB;
+      int blkj = 0;
+      for (; blkj < NB - 1; ++blkj) {
+        const int c = __popcll(mk[blkj]);
+        if (jj < c) break;
+        jj -= c;
+      }
+      const int bit = nth_bit64(mk[blkj], jj);
+      const int x = ox + (blkj % NBX) * SWR_BLOCK + (bit & 7);
+      const int y = oy + (blkj / NBX) * SWR_BLOCK + (bit >> 3);
+      const float* r = srec + k * RL::R;
+      const bool blockmode = __float_as_int(r[0]) & 2;
+      float fx, fy;
+      int ka, kb;
+      if (blockmode) {
+        fx = swr_add((float)(x & ~7), 0.5f);
+        fy = swr_add((float)(y & ~7), 0.5f);
+        ka = x & 7;
+        kb = y & 7;
+      } else {
+        const int2 sp = sspan[k * TILE + (y - oy)];
+        fx = swr_add((float)sp.x, 0.5f);
+        fy = swr_add((float)y, 0.5f);
+        ka = x - sp.x;
+        kb = 0;
+      }
+      const float* eq = r + RL::EQ0;
+      GpuPixel<PS> pd;
+      pd.x = x;
+      pd.y = y;
+      pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
+      build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
+      sfz[f] = pd.z;
+      sfc[f] = PS::shade(pd, g.draws[__float_as_int(r[1])].u);
+    }
+    __syncthreads();
+    // C2: fragments in primitive order
     for (int k = 0; k < n; ++k) {
       const float* r = srec + k * RL::R;
       const int flags = __float_as_int(r[0]);
       if (!(flags & 1)) continue;
       const bool blockmode = flags & 2;
-      const float* eq = r + RL::EQ0;
+      const bool comp = scomp[k];
+      const uint64_t* mk = smask + k * NB;
 #pragma unroll
       for (int q = 0; q < PPT; ++q) {
         if (!in[q]) continue;
+        const uint64_t m = mk[blk[q]];
+        const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+        if (!((m >> bit) & 1ull)) continue;
+        frags++;
+        if (comp) {
+          int rank = __popcll(m & ((1ull << bit) - 1ull));
+          for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
+          const int f = (int)sex[k] + rank;
+          PS::apply(st[q], sfz[f], sfc[f], (int)sids[k]);
+          continue;
+        }
         float fx, fy;
         int ka, kb;
         if (blockmode) {
-          const uint64_t m = smask[k * NB + blk[q]];
-          if (!((m >> ((py[q] & 7) * 8 + (px[q] & 7))) & 1ull)) continue;
           fx = swr_add((float)(px[q] & ~7), 0.5f);
           fy = swr_add((float)(py[q] & ~7), 0.5f);
           ka = px[q] & 7;
           kb = py[q] & 7;
         } else {
           const int2 sp = sspan[k * TILE + (py[q] - oy)];
-          if (px[q] < sp.x || px[q] >= sp.y) continue;
           fx = swr_add((float)sp.x, 0.5f);
           fy = swr_add((float)py[q], 0.5f);
           ka = px[q] - sp.x;
           kb = 0;
         }
+        const float* eq = r + RL::EQ0;
         GpuPixel<PS> pd;
         pd.x = px[q];
         pd.y = py[q];
-        if (RL::IZ) {
-          const float* q3 = eq + 3 * RL::EQ_Z;
-          const float z0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-          pd.z = blockmode ? fold7(z0, q3[0], ka) : swr_fold(z0, q3[0], ka);
-          frags++;
-          if (PS::earlyReject(pd.z, st[q])) continue;
-        } else {
-          frags++;
-        }
-        if (RL::IW) {
-          const float* q3 = eq + 3 * RL::EQ_W;
-          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-          pd.invw = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
-          pd.w = swr_div(1.0f, pd.invw);
-        }
-#pragma unroll
-        for (int i = 0; i < RL::NA; ++i) {
-          const float* q3 = eq + 3 * (RL::EQ_A + i);
-          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-          pd.avar[i] = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
-        }
-#pragma unroll
-        for (int i = 0; i < RL::NP; ++i) {
-          const float* q3 = eq + 3 * (RL::EQ_P + i);
-          const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-          const float pt = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
-          pd.pvar[i] = swr_mul(pt, pd.w);
-        }
+        pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
+        if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
+        build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
         PS::drawPixel(pd, (int)sids[k], st[q], g.draws[__float_as_int(r[1])].u);
       }
     }

@@ -22,7 +22,7 @@ void run_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
 
 template <class VS>
 void run_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<nbatches, 256, 0, s>>>(a);
+  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<nbatches, SWR_BATCH_PRIMS, 0, s>>>(a);
 }
 
 template <class VS>
