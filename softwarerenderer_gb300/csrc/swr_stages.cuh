@@ -768,51 +768,52 @@ __device__ __forceinline__ float fold7(float v, float a, int k) {
   return v;
 }
 
-// Exact 8x8 coverage mask of one block (Rasterizer.h:263-304 classification, then
-// PixelShaderBase::drawBlock<TestEdges> per-pixel tests with EdgeData stepping,
-// PixelShaderBase.h:64-93): bit r*8+c set when pixel (bx+c, by+r) reaches drawPixel.
-__device__ __forceinline__ uint64_t block_mask(const float* r, int flags, int bx, int by) {
+// Block classification of Rasterizer.h:263-304 for the block at (bx, by): 0 = skipped,
+// 1 = drawBlock<false> (every pixel), 2 = drawBlock<true> (per-pixel edge tests).
+__device__ __forceinline__ int block_class(const float* r, int flags, int bx, int by) {
   const float fx = swr_add((float)bx, 0.5f), fy = swr_add((float)by, 0.5f);
   const float s = (float)(SWR_BLOCK - 1);
-  float ev[3];
   bool t00[3], t01[3], t10[3], t11[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     const float ea = r[6 + 3 * j], eb = r[7 + 3 * j], ec = r[8 + 3 * j];
     const bool tie = (flags >> (2 + j)) & 1;
-    ev[j] = swr_eval(ea, eb, ec, fx, fy);
-    const float v01 = swr_add(ev[j], swr_mul(eb, s));
-    const float v10 = swr_add(ev[j], swr_mul(ea, s));
+    const float ev = swr_eval(ea, eb, ec, fx, fy);
+    const float v01 = swr_add(ev, swr_mul(eb, s));
+    const float v10 = swr_add(ev, swr_mul(ea, s));
     const float v11 = swr_add(v01, swr_mul(ea, s));
-    t00[j] = edge_test(ev[j], tie);
+    t00[j] = edge_test(ev, tie);
     t01[j] = edge_test(v01, tie);
     t10[j] = edge_test(v10, tie);
     t11[j] = edge_test(v11, tie);
   }
   const int inside = (t00[0] && t00[1] && t00[2]) + (t01[0] && t01[1] && t01[2]) +
                      (t10[0] && t10[1] && t10[2]) + (t11[0] && t11[1] && t11[2]);
-  if (inside == 4) return ~0ull;  // drawBlock<false>: every pixel
+  if (inside == 4) return 1;
   if (inside == 0) {
     const bool s00 = (t00[0] == t00[1]) == t00[2], s01 = (t01[0] == t01[1]) == t01[2];
     const bool s10 = (t10[0] == t10[1]) == t10[2], s11 = (t11[0] == t11[1]) == t11[2];
-    if (s00 && s01 && s10 && s11) return 0ull;  // skipped
+    if (s00 && s01 && s10 && s11) return 0;
   }
-  // drawBlock<true>: row starts step by b, pixels step by a
+  return 2;
+}
+
+// Row `row` of drawBlock<true> (PixelShaderBase.h:64-93): the row start is the block
+// corner's edge value stepped `row` times by b (eo.stepY), pixels step by a (ei.stepX).
+// Returns the row's 8 coverage bits.
+__device__ __forceinline__ uint32_t block_row_bits(const float* r, int flags, int bx, int by, int row) {
+  const float fx = swr_add((float)bx, 0.5f), fy = swr_add((float)by, 0.5f);
   const bool tie0 = (flags >> 2) & 1, tie1 = (flags >> 3) & 1, tie2 = (flags >> 4) & 1;
-  float o0 = ev[0], o1 = ev[1], o2 = ev[2];
-  uint64_t m = 0;
-  for (int row = 0; row < SWR_BLOCK; ++row) {
-    float i0 = o0, i1 = o1, i2 = o2;
+  float i0 = fold7(swr_eval(r[6], r[7], r[8], fx, fy), r[7], row);
+  float i1 = fold7(swr_eval(r[9], r[10], r[11], fx, fy), r[10], row);
+  float i2 = fold7(swr_eval(r[12], r[13], r[14], fx, fy), r[13], row);
+  uint32_t m = 0;
 #pragma unroll
-    for (int col = 0; col < SWR_BLOCK; ++col) {
-      if (edge_test(i0, tie0) && edge_test(i1, tie1) && edge_test(i2, tie2)) m |= 1ull << (row * 8 + col);
-      i0 = swr_add(i0, r[6]);
-      i1 = swr_add(i1, r[9]);
-      i2 = swr_add(i2, r[12]);
-    }
-    o0 = swr_add(o0, r[7]);
-    o1 = swr_add(o1, r[10]);
-    o2 = swr_add(o2, r[13]);
+  for (int col = 0; col < SWR_BLOCK; ++col) {
+    if (edge_test(i0, tie0) && edge_test(i1, tie1) && edge_test(i2, tie2)) m |= 1u << col;
+    i0 = swr_add(i0, r[6]);
+    i1 = swr_add(i1, r[9]);
+    i2 = swr_add(i2, r[12]);
   }
   return m;
 }
@@ -870,9 +871,10 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 
 // One CTA per screen tile, 256 threads.  Per chunk of CH primitives of the tile's bin:
 //   A. stage the setup records in shared memory;
-//   B. one thread per (primitive, 8x8 block) computes the exact coverage mask: Block mode
-//      by the reference's corner classification and stepped edge tests, Span mode from the
-//      rows' [xl, xr) (also kept as the interpolation start of each row);
+//   B. exact coverage masks per (primitive, 8x8 block): one thread per pair classifies
+//      Block-mode blocks (the reference's corner test) and builds Span-mode rows from
+//      [xl, xr) (kept as each row's interpolation start); partially covered blocks are then
+//      finished by 8 lanes each, one row per lane, with the reference's stepped edge tests;
 //   C1. small primitives (<= 64 covered pixels in the tile, up to FB fragments per chunk)
 //      are compacted: one thread per covered fragment rebuilds the stepped interpolants and
 //      evaluates the pixel shader's pure shade() at full SIMT width;
@@ -900,6 +902,8 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
   __shared__ Color sfc[FB];
   __shared__ uint32_t sfr[32];
   __shared__ uint32_t snc;
+  __shared__ uint16_t spart[CH * NB];  // partially covered (primitive, block) pairs
+  __shared__ uint32_t snpart;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t tile = blockIdx.x;
   const uint32_t b = g.tile_start[tile], e = g.tile_start[tile + 1];
@@ -943,7 +947,10 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
       }
     }
     __syncthreads();
-    // B: coverage per (primitive, block)
+    // B1: coverage per (primitive, block).  Fully covered / skipped blocks and Span rows are
+    // finished here; partially covered Block-mode blocks are queued for B2.
+    if (threadIdx.x == 0) snpart = 0;
+    __syncthreads();
     for (int i = threadIdx.x; i < n * NB; i += 256) {
       const int k = i / NB, j = i - k * NB;
       const float* r = srec + k * RL::R;
@@ -953,7 +960,11 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
       const bool hit = (flags & 1) && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
                        by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]);
       if (flags & 2) {
-        if (hit) m = block_mask(r, flags, bx, by);
+        if (hit) {
+          const int cls = block_class(r, flags, bx, by);
+          if (cls == 1) m = ~0ull;
+          if (cls == 2) spart[atomicAdd(&snpart, 1u)] = (uint16_t)i;
+        }
       } else if (flags & 1) {
         const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
         for (int rr = 0; rr < SWR_BLOCK; ++rr) {
@@ -979,6 +990,28 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
         }
       }
       smask[i] = m;
+    }
+    __syncthreads();
+    // B2: partially covered blocks, one row per lane (8 lanes per block)
+    {
+      const int np8 = (int)snpart * SWR_BLOCK;
+      for (int t0 = 0; t0 < np8; t0 += 256) {
+        const int t = t0 + threadIdx.x;
+        uint64_t bits = 0;
+        int i = 0;
+        if (t < np8) {
+          i = spart[t >> 3];
+          const int row = t & 7;
+          const int k = i / NB, j = i - k * NB;
+          const float* r = srec + k * RL::R;
+          bits = (uint64_t)block_row_bits(r, __float_as_int(r[0]), ox + (j % NBX) * SWR_BLOCK,
+                                          oy + (j / NBX) * SWR_BLOCK, row) << (row * 8);
+        }
+        bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+        bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
+        bits |= __shfl_xor_sync(0xffffffffu, bits, 4);
+        if (t < np8 && (t & 7) == 0) smask[i] = bits;
+      }
     }
     __syncthreads();
     // C1 set-up: compact the small primitives' fragments (a prefix of the chunk's small
@@ -1048,28 +1081,35 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
       sfc[f] = PS::shade(pd, g.draws[__float_as_int(r[1])].u);
     }
     __syncthreads();
-    // C2: fragments in primitive order
-    for (int k = 0; k < n; ++k) {
-      const float* r = srec + k * RL::R;
-      const int flags = __float_as_int(r[0]);
-      if (!(flags & 1)) continue;
-      const bool blockmode = flags & 2;
-      const bool comp = scomp[k];
-      const uint64_t* mk = smask + k * NB;
+    // C2: fragments in primitive order.  Each warp owns one 8 x 4 half block per sub-tile
+    // q; a ballot over the chunk gives the primitives whose masks touch it, visited in
+    // increasing order (per-pixel order = primitive order).
 #pragma unroll
-      for (int q = 0; q < PPT; ++q) {
-        if (!in[q]) continue;
+    for (int q = 0; q < PPT; ++q) {
+      const int half = (py[q] >> 2) & 1;
+      uint64_t hits = 0;
+      for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        const bool h = k < n && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
+        hits |= (uint64_t)__ballot_sync(0xffffffffu, h) << k0;
+      }
+      const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+      while (hits) {
+        const int k = __ffsll((long long)hits) - 1;
+        hits &= hits - 1ull;
+        const uint64_t* mk = smask + k * NB;
         const uint64_t m = mk[blk[q]];
-        const int bit = (py[q] & 7) * 8 + (px[q] & 7);
-        if (!((m >> bit) & 1ull)) continue;
+        if (!in[q] || !((m >> bit) & 1ull)) continue;
+        const float* r = srec + k * RL::R;
         frags++;
-        if (comp) {
+        if (scomp[k]) {
           int rank = __popcll(m & ((1ull << bit) - 1ull));
           for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
           const int f = (int)sex[k] + rank;
           PS::apply(st[q], sfz[f], sfc[f], (int)sids[k]);
           continue;
         }
+        const bool blockmode = __float_as_int(r[0]) & 2;
         float fx, fy;
         int ka, kb;
         if (blockmode) {
