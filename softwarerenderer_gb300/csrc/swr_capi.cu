@@ -78,7 +78,7 @@ struct swr_context {
   swr::Buffer draws, targets, draw_vbase, draw_bbase, target_tile_base;
   swr::Buffer ptv, clipv, clip_table, clip_slot, tri_flags, batch_counts, batch_base;
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
-  swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs;
+  swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start;
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
   // tracing: CUDA events at the stage boundaries of every draw since the last
@@ -140,7 +140,7 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->clip_slot.ensure((size_t)nsub * 4 + 16);
   ok &= c->tri_flags.ensure((size_t)nsub + 16);
   ok &= c->lp_refs.ensure((size_t)nsub * 8 + 16);
-  ok &= c->batch_counts.ensure((size_t)nbatches * 8 + 16);
+  ok &= c->batch_counts.ensure((size_t)nbatches * 16 + 16);  // per half batch (points/lines: per batch)
   ok &= c->batch_base.ensure((size_t)nbatches * 4 + 16);
   ok &= c->tris.ensure((size_t)c->cap_prims * 16 + 16);
   ok &= c->recs.ensure((size_t)c->cap_prims * R * 4 + 16);
@@ -151,7 +151,9 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->keys1.ensure((size_t)c->cap_pairs * 4 + 16);
   ok &= c->vals1.ensure((size_t)c->cap_pairs * 4 + 16);
   ok &= c->tile_start.ensure((size_t)(ntiles + 1) * 4 + 16);
-  const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64;
+  ok &= c->cell_count.ensure((size_t)ntiles * SWR_SEGS * 4 + 16);
+  ok &= c->cell_start.ensure(((size_t)ntiles * SWR_SEGS + 1) * 4 + 16);
+  const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64 + 2 * scan_scratch_words(ntiles * SWR_SEGS);
   ok &= c->scratch.ensure(sw * 4);
   ok &= c->draws.ensure(sizeof(SwrDrawDesc));
   ok &= c->targets.ensure(sizeof(SwrTargetDesc));
@@ -184,10 +186,18 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
 }
 
 // Setup, binning and tile raster for the primitives in c->tris (count on the device).
+// Binning: setup counts (tile, primitive segment) cells, a scan turns the counts into
+// offsets, k_fill_bins scatters primitive ids into their cells, k_sort_cells restores the
+// primitive order inside each cell; a tile's bin is then its cells' contiguous range.
 int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int vs_a, int vs_p,
                  uint32_t ntiles, cudaStream_t s) {
   uint32_t* st = c->status.as<uint32_t>();
+  const uint32_t ncells = ntiles * SWR_SEGS;
+  int seg_shift = 0;
+  while (((uint64_t)(c->cap_prims > 0 ? c->cap_prims - 1 : 0) >> seg_shift) >= SWR_SEGS) ++seg_shift;
+  cudaMemsetAsync(c->cell_count.p, 0, (size_t)ncells * 4, s);
   SetupArgs sa;
+  memset(&sa, 0, sizeof(sa));
   sa.tris = c->tris.as<uint4>();
   sa.status = st;
   sa.cap_prims = c->cap_prims;
@@ -203,26 +213,25 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   sa.recs = c->recs.as<float>();
   sa.tile_count = c->tile_count.as<uint32_t>();
   sa.tile = c->tile;
+  sa.cell_count = c->cell_count.as<uint32_t>();
+  sa.seg_shift = seg_shift;
   ps->setup(sa, s);
   mark(c, 3, s);
   uint32_t* scr = c->scratch.as<uint32_t>();
-  uint32_t* sort_scr = scr + scan_scratch_words(c->cap_prims) + 32;
-  scan_exclusive(c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(), st + SWR_ST_PRIMS, c->cap_prims,
-                 st + SWR_ST_PAIRS, scr, s);
-  ps->emit_pairs(st, c->cap_prims, c->recs.as<float>(), c->tile_count.as<uint32_t>(), c->pair_off.as<uint32_t>(),
-                 st + SWR_ST_PAIRS, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
-                 c->tile, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), st, s);
-  const int which = radix_sort_pairs(c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), c->keys1.as<uint32_t>(),
-                                     c->vals1.as<uint32_t>(), st + SWR_ST_PAIRS, c->cap_pairs,
-                                     bits_for(ntiles), sort_scr, s);
-  uint32_t* keys = which ? c->keys1.as<uint32_t>() : c->keys0.as<uint32_t>();
-  uint32_t* vals = which ? c->vals1.as<uint32_t>() : c->vals0.as<uint32_t>();
-  segment_starts(keys, st + SWR_ST_PAIRS, c->cap_pairs, ntiles, c->tile_start.as<uint32_t>(), s);
+  uint32_t* cstart = c->cell_start.as<uint32_t>();
+  scan_exclusive(c->cell_count.as<uint32_t>(), cstart, nullptr, ncells, cstart + ncells, scr, s);
+  ps->fill_bins(st, c->cap_prims, c->recs.as<float>(), c->tile_count.as<uint32_t>(), c->cell_count.as<uint32_t>(),
+                cstart, ncells, seg_shift, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
+                c->tile, c->keys0.as<uint32_t>(), st, s);
+  const uint32_t warps_per_block = 8;
+  k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
+      st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>());
   mark(c, 4, s);
   RasterArgs ra;
   ra.status = st;
-  ra.tile_start = c->tile_start.as<uint32_t>();
-  ra.bin = vals;
+  ra.tile_start = cstart;
+  ra.tile_stride = SWR_SEGS;
+  ra.bin = c->vals0.as<uint32_t>();
   ra.recs = c->recs.as<float>();
   ra.draws = c->draws.as<SwrDrawDesc>();
   ra.targets = c->targets.as<SwrTargetDesc>();
@@ -232,8 +241,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
   k_close_draw<<<1, 1, 0, s>>>(st);
-  const int passes = (bits_for(ntiles) + 7) / 8;
-  c->launches += 1 + 2 + 1 + 3 * passes + 1 + (ntiles ? 1 : 0) + 1;
+  c->launches += 1 + 2 + 1 + 1 + (ntiles ? 1 : 0) + 1;
   return cuda_err(cudaGetLastError());
 }
 

@@ -7,6 +7,7 @@
 #define SWR_BATCH_PRIMS 1024  // VertexProcessor flushes every 1024 primitives (VertexProcessor.cpp:110-116)
 #define SWR_BLOCK 8           // swr::BlockSize (IRasterizer.h:33)
 #define SWR_CLIP_REF 0x80000000u  // vertex references with this bit address the clip-vertex buffer
+#define SWR_SEGS 32               // primitive segments of the binning (cells per tile)
 
 // Status word layout (device memory, reset by every submission).
 enum SwrStatusWord {

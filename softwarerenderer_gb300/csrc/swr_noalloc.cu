@@ -175,6 +175,7 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
     k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, 3, (uint32_t)nverts, keep, pos, tris, st);
   }
   SetupArgs sa;
+  memset(&sa, 0, sizeof(sa));  // no cell counting: this path bins with the radix sort
   sa.tris = tris;
   sa.status = st;
   sa.cap_prims = kMaxTris;
@@ -203,6 +204,7 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   RasterArgs ra;
   ra.status = st;
   ra.tile_start = tile_start;
+  ra.tile_stride = 1;
   ra.bin = vals;
   ra.recs = recs;
   ra.draws = dd;

@@ -30,6 +30,15 @@ void run_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs, co
 }
 
 template <class PS>
+void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+              uint32_t* cell_count, const uint32_t* cell_start, uint32_t ncells, int seg_shift, uint32_t cap_pairs,
+              const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* bin, uint32_t* status_w,
+              cudaStream_t s) {
+  k_fill_bins<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, cell_count, cell_start, ncells,
+                                        seg_shift, cap_pairs, draws, targets, tile, bin, status_w);
+}
+
+template <class PS>
 void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
   if (!ntiles) return;
   if (tile == 32) k_raster<PS, 32, kChunk><<<ntiles, 256, 0, s>>>(a);
@@ -62,6 +71,7 @@ PsOps make() {
   o.setup = &run_setup<PS>;
   o.emit_pairs = &run_pairs<PS>;
   o.raster = &run_raster<PS>;
+  o.fill_bins = &run_fill<PS>;
   o.lp_R = LpRec<PS>::R;
   o.lp_setup = &run_lp_setup<PS>;
   o.lp_frags = &run_lp_frags<PS>;

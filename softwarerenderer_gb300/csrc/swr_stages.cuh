@@ -289,28 +289,33 @@ __device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, uint32
   ex_kept = __popc(keep >> 1);
 }
 
-// The batch's 3 x 1024 indices, loaded cooperatively (coalesced) into shared memory.
-__device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uint32_t p0, uint32_t* sidx) {
-  const uint32_t n = min((uint32_t)SWR_BATCH_PRIMS, D.nprims - p0);
+// Triangles [p0, p0 + count) of a draw (clamped to the draw): their 3 indices each are
+// loaded cooperatively (coalesced) into shared memory.  Returns the clamped count.
+__device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uint32_t p0, uint32_t* sidx,
+                                                       uint32_t count = SWR_BATCH_PRIMS) {
+  const uint32_t n = p0 < D.nprims ? min(count, D.nprims - p0) : 0u;
   const uint32_t* src = D.indices + (size_t)3 * p0;
   for (uint32_t i = threadIdx.x; i < 3 * n; i += blockDim.x) sidx[i] = src[i];
   __syncthreads();
   return n;
 }
 
+#define SWR_HALF (SWR_BATCH_PRIMS / 2)  // triangles per assembly CTA (half a batch)
+
+// One CTA per half batch (512 triangles, 2 per thread): clip / cull and count the
+// survivors: half_counts[h] = (kept input slots, kept extra fan triangles).
 template <int A, int P>
 __global__ void __launch_bounds__(256) k_assemble_count(AssembleArgs g) {
   __shared__ uint32_t tmp[32];
-  __shared__ uint32_t sidx[3 * SWR_BATCH_PRIMS];
-  const uint32_t b = blockIdx.x;
+  __shared__ uint32_t sidx[3 * SWR_HALF];
+  const uint32_t hb = blockIdx.x, b = hb >> 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
-  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
-  const uint32_t n = load_batch_indices(D, p0, sidx);
-  // four triangles per thread, strided so a warp's triangles are consecutive
+  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + (hb & 1) * SWR_HALF;
+  const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
   uint32_t in_sum = 0, ex_sum = 0;
-  for (int j = 0; j < 4; ++j) {
-    const uint32_t q = j * 256 + threadIdx.x;
+  for (int j = 0; j < 2; ++j) {
+    const uint32_t q = threadIdx.x * 2 + j;
     if (q < n) {
       uint32_t ik, ek;
       assemble_one<A, P>(g, D, p0 + q, sidx[3 * q], sidx[3 * q + 1], sidx[3 * q + 2], ik, ek);
@@ -321,7 +326,7 @@ __global__ void __launch_bounds__(256) k_assemble_count(AssembleArgs g) {
   uint32_t tin, tex;
   swr_block_exscan(in_sum, tmp, &tin);
   swr_block_exscan(ex_sum, tmp, &tex);
-  if (threadIdx.x == 0) g.batch_counts[b] = make_uint2(tin, tex);
+  if (threadIdx.x == 0) g.batch_counts[hb] = make_uint2(tin, tex);
 }
 
 // Exclusive scan of per-batch totals -> batch bases; primitive total into the status word.
@@ -347,59 +352,68 @@ static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts,
 // batch base is the sum of the totals of the batches before it; the last batch publishes
 // the primitive count (and flags an undersized primitive queue).
 template <int A, int P>
-__global__ void __launch_bounds__(SWR_BATCH_PRIMS) k_assemble_emit(AssembleArgs g) {
+__global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
   __shared__ uint32_t tmp[32];
-  __shared__ uint32_t sidx[3 * SWR_BATCH_PRIMS];
+  __shared__ uint32_t sidx[3 * SWR_HALF];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
-  const uint32_t b = blockIdx.x;
+  const uint32_t hb = blockIdx.x, b = hb >> 1, half = hb & 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
-  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS;
-  const uint32_t n = load_batch_indices(D, p0, sidx);
+  const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + half * SWR_HALF;
+  const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
   uint32_t before = 0;
-  for (uint32_t i = threadIdx.x; i < b; i += blockDim.x) before += g.batch_counts[i].x + g.batch_counts[i].y;
+  for (uint32_t i = threadIdx.x; i < 2 * b; i += blockDim.x) before += g.batch_counts[i].x + g.batch_counts[i].y;
   uint32_t base;
   swr_block_exscan(before, tmp, &base);
-  const uint32_t q = threadIdx.x;
-  uint32_t fl = 0, slot = 0xffffffffu;
-  uint32_t keep = 0;
-  if (q < n) {
-    fl = g.tri_flags[D.pbase + p0 + q];
-    if (fl & 4) {
-      slot = g.clip_slot[D.pbase + p0 + q];
-      if (slot != 0xffffffffu) keep = g.clip_table[slot].keep;
-    } else {
-      keep = fl & 1;
+  const uint2 c0 = g.batch_counts[2 * b], c1 = g.batch_counts[2 * b + 1];
+  const uint32_t batch_in = c0.x + c1.x, batch_total = batch_in + c0.y + c1.y;
+  // effective order within the batch: every kept input slot (first half, then second),
+  // then every extra fan triangle (first half's, then second's)
+  const uint32_t in_base = base + (half ? c0.x : 0u);
+  const uint32_t ex_base = base + batch_in + (half ? c0.y : 0u);
+  uint32_t fl[2] = {0, 0}, slot[2] = {0xffffffffu, 0xffffffffu}, keep[2] = {0, 0};
+  uint32_t in_sum = 0, ex_sum = 0;
+  for (int j = 0; j < 2; ++j) {
+    const uint32_t q = threadIdx.x * 2 + j;
+    if (q < n) {
+      fl[j] = g.tri_flags[D.pbase + p0 + q];
+      if (fl[j] & 4) {
+        slot[j] = g.clip_slot[D.pbase + p0 + q];
+        if (slot[j] != 0xffffffffu) keep[j] = g.clip_table[slot[j]].keep;
+      } else {
+        keep[j] = fl[j] & 1;
+      }
+      in_sum += keep[j] & 1u;
+      ex_sum += __popc(keep[j] >> 1);
     }
   }
   uint32_t tin, tex;
-  uint32_t rin = swr_block_exscan(keep & 1u, tmp, &tin);
-  uint32_t rex = swr_block_exscan(__popc(keep >> 1), tmp, &tex);
-  if (b == gridDim.x - 1 && threadIdx.x == 0) {
-    g.status[SWR_ST_PRIMS] = base + tin + tex;
-    if (base + tin + tex > g.cap_prims) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
+  uint32_t rin = swr_block_exscan(in_sum, tmp, &tin) + in_base;
+  uint32_t rex = swr_block_exscan(ex_sum, tmp, &tex) + ex_base;
+  if (hb == gridDim.x - 1 && threadIdx.x == 0) {
+    g.status[SWR_ST_PRIMS] = base + batch_total;
+    if (base + batch_total > g.cap_prims) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
   }
-  if (base + tin + tex > g.cap_prims) {
+  if (base + batch_total > g.cap_prims) {
     if (threadIdx.x == 0) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
     return;
   }
-  if (!keep) return;
-  if (!(fl & 4)) {
-    uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
-    if (fl & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
-    g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
-  } else {
-    // first fan triangle in the input slot, the others after all of the batch's slots
-    const SwrClipEntry e = g.clip_table[slot];
-    for (int k = 0; k + 2 < e.n; ++k) {
-      if (!((e.keep >> k) & 1)) continue;
-      uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
-      if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
-      if (k == 0) {
-        g.tris[base + rin] = make_uint4(r0, r1, r2, (uint32_t)d);
-      } else {
-        g.tris[base + tin + rex] = make_uint4(r0, r1, r2, (uint32_t)d);
-        rex++;
+  for (int j = 0; j < 2; ++j) {
+    const uint32_t q = threadIdx.x * 2 + j;
+    if (!keep[j]) continue;
+    if (!(fl[j] & 4)) {
+      uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
+      if (fl[j] & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
+      g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
+    } else {
+      // first fan triangle in the input slot, the others after all of the batch's slots
+      const SwrClipEntry e = g.clip_table[slot[j]];
+      for (int k = 0; k + 2 < e.n; ++k) {
+        if (!((e.keep >> k) & 1)) continue;
+        uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
+        if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
+        if (k == 0) g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
+        else g.tris[rex++] = make_uint4(r0, r1, r2, (uint32_t)d);
       }
     }
   }
@@ -496,6 +510,8 @@ struct SetupArgs {
   float* recs;
   uint32_t* tile_count;
   int tile;  // tile edge in pixels
+  uint32_t* cell_count;  // per (tile, primitive segment): bin entries (counted with atomics)
+  int seg_shift;         // primitive segment = primitive index >> seg_shift (< SWR_SEGS)
 };
 
 struct SpanHalf {
@@ -683,6 +699,12 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
       if (bx0 <= bx1 && by0 <= by1) {
         const int tx0 = bx0 / g.tile, tx1 = bx1 / g.tile, ty0 = by0 / g.tile, ty1 = by1 / g.tile;
         tiles = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+        if (g.cell_count) {
+          const uint32_t seg = p >> g.seg_shift;
+          for (int ty = ty0; ty <= ty1; ++ty)
+            for (int tx = tx0; tx <= tx1; ++tx)
+              atomicAdd(&g.cell_count[(T.tile_base + (uint32_t)(ty * T.tiles_x + tx)) * SWR_SEGS + seg], 1u);
+        }
       } else {
         flags = 0;
       }
@@ -737,6 +759,99 @@ __global__ void __launch_bounds__(256) k_emit_pairs(const uint32_t* status, uint
   }
 }
 
+// Segmented binning.  The primitive list is cut into SWR_SEGS contiguous segments; a
+// (tile, segment) cell holds the segment's primitives that touch the tile.  Cells are laid
+// out tile-major, so a tile's bin is one contiguous range ordered by segment; inside a cell
+// the fill order is arbitrary and k_sort_cells restores increasing primitive order.
+template <class PS>
+__global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint32_t cap_prims, const float* recs,
+                                                   const uint32_t* tile_count, uint32_t* cell_count,
+                                                   const uint32_t* cell_start, uint32_t ncells, int seg_shift,
+                                                   uint32_t cap_pairs, const SwrDrawDesc* draws,
+                                                   const SwrTargetDesc* targets, int tile, uint32_t* bin,
+                                                   uint32_t* status_w) {
+  typedef Rec<PS> RL;
+  if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  const uint32_t total = cell_start[ncells];
+  if (total > cap_pairs) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicOr(&status_w[SWR_ST_FLAGS], SWR_F_PAIR_OVERFLOW);
+      status_w[SWR_ST_PAIRS] = total;
+    }
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) status_w[SWR_ST_PAIRS] = total;
+  uint32_t np = status[SWR_ST_PRIMS];
+  if (np > cap_prims) np = cap_prims;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    if (!tile_count[p]) continue;
+    const float* rec = recs + (size_t)p * RL::R;
+    const SwrTargetDesc& T = targets[draws[__float_as_int(rec[1])].target];
+    const int tx0 = __float_as_int(rec[2]) / tile, ty0 = __float_as_int(rec[3]) / tile;
+    const int tx1 = __float_as_int(rec[4]) / tile, ty1 = __float_as_int(rec[5]) / tile;
+    const uint32_t seg = p >> seg_shift;
+    for (int ty = ty0; ty <= ty1; ++ty)
+      for (int tx = tx0; tx <= tx1; ++tx) {
+        const uint32_t cell = (T.tile_base + (uint32_t)(ty * T.tiles_x + tx)) * SWR_SEGS + seg;
+        const uint32_t pos = atomicSub(&cell_count[cell], 1u) - 1u;
+        bin[cell_start[cell] + pos] = p;
+      }
+  }
+}
+
+// One warp per tile: every cell of the tile is copied to `out` in increasing primitive
+// order.  Lane c owns cell c: cells of up to 16 entries are sorted in registers by the
+// lane; larger cells are ranked by the whole warp (primitive ids are unique).
+static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* status, const uint32_t* cell_start,
+                                                          uint32_t ntiles, uint32_t cap_pairs, const uint32_t* in,
+                                                          uint32_t* out) {
+  if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  if (cell_start[(size_t)ntiles * SWR_SEGS] > cap_pairs) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= ntiles) return;
+  const uint32_t s = cell_start[(size_t)t * SWR_SEGS + lane];
+  const uint32_t last = cell_start[(size_t)t * SWR_SEGS + SWR_SEGS];
+  // every lane takes part in the shuffle; lane 31 then uses the next tile's first start
+  const uint32_t nxt = __shfl_down_sync(0xffffffffu, s, 1);
+  const uint32_t e = lane < SWR_SEGS - 1 ? nxt : last;
+  // starts are an exclusive scan (monotone, bounded by the total <= cap_pairs); anything
+  // else leaves the cell empty instead of walking a wrapped length
+  const uint32_t m = (e >= s && e <= cap_pairs) ? e - s : 0u;
+  constexpr int kSmall = 16;
+  if (m <= kSmall) {
+    uint32_t v[kSmall];
+#pragma unroll
+    for (int i = 0; i < kSmall; ++i) v[i] = (uint32_t)i < m ? in[s + i] : 0xffffffffu;
+    // odd-even transposition network on 16 registers
+#pragma unroll
+    for (int r = 0; r < kSmall; ++r)
+#pragma unroll
+      for (int i = r & 1; i + 1 < kSmall; i += 2)
+        if (v[i] > v[i + 1]) { const uint32_t x = v[i]; v[i] = v[i + 1]; v[i + 1] = x; }
+#pragma unroll
+    for (int i = 0; i < kSmall; ++i)
+      if ((uint32_t)i < m) out[s + i] = v[i];
+  }
+  uint32_t big = __ballot_sync(0xffffffffu, m > kSmall);
+  while (big) {
+    const int c = __ffs(big) - 1;
+    big &= big - 1u;
+    const uint32_t cs = __shfl_sync(0xffffffffu, s, c), cm = __shfl_sync(0xffffffffu, m, c);
+    for (uint32_t i0 = 0; i0 < cm; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const uint32_t val = i < cm ? in[cs + i] : 0xffffffffu;
+      uint32_t rank = 0;
+      for (uint32_t j0 = 0; j0 < cm; j0 += 32) {
+        const uint32_t w = j0 + lane < cm ? in[cs + j0 + lane] : 0xffffffffu;
+#pragma unroll 8
+        for (int l = 0; l < 32; ++l) rank += __shfl_sync(0xffffffffu, w, l) < val;
+      }
+      if (i < cm) out[cs + rank] = val;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------
 // Tile rasterization.
 
@@ -750,8 +865,9 @@ struct GpuPixel {  // PixelData (PixelData.h:35-146) as seen by drawPixel
 
 struct RasterArgs {
   const uint32_t* status;
-  const uint32_t* tile_start;  // per global tile, plus one
-  const uint32_t* bin;         // primitive ids sorted by tile
+  const uint32_t* tile_start;  // bin start of tile t at tile_start[t * tile_stride] (plus the end)
+  uint32_t tile_stride;        // 1 for per-tile starts, SWR_SEGS for per-(tile, segment) cells
+  const uint32_t* bin;         // primitive ids, each tile's range in increasing order
   const float* recs;
   const SwrDrawDesc* draws;
   const SwrTargetDesc* targets;
@@ -906,7 +1022,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
   __shared__ uint32_t snpart;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t tile = blockIdx.x;
-  const uint32_t b = g.tile_start[tile], e = g.tile_start[tile + 1];
+  const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
   if (b == e) return;
   const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
   const SwrTargetDesc& T = g.targets[ti];
