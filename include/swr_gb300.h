@@ -96,6 +96,33 @@ int swr_set_uniforms(swr_context* ctx, const struct SwrUniforms* u);
 int swr_draw_list(swr_context* ctx, int mode, const float* vertices, uint64_t nverts,
                   const int32_t* indices, uint64_t count, void* stream);
 
+/* Batched rendering (no reference counterpart: the reference draws one mesh per
+ * drawElements call).  One item is the state of one VertexProcessor::drawElements
+ * (VertexProcessor.cpp:78-120) call with DrawMode::Triangle; all items of a batch use the
+ * same vertex and pixel shader.  Items whose uniforms name the same colour buffer draw
+ * into one shared target in item order; every other item gets its own target.  The whole
+ * batch is one pass of the pipeline (every kernel covers all items), so per-item results
+ * equal separate swr_draw_elements calls. */
+typedef struct swr_draw_item {
+  int32_t vs_id, ps_id;
+  int32_t cull_mode, raster_mode;
+  int32_t viewport[4];
+  float depth_range[2];
+  int32_t scissor[4];
+  const void* attrib[8];
+  int32_t attrib_stride[8];
+  uint64_t attrib_bytes[8];
+  const uint32_t* indices;
+  uint64_t count;
+  const struct SwrUniforms* uniforms;
+} swr_draw_item;
+
+int swr_draw_batch(swr_context* ctx, const swr_draw_item* items, int n, void* stream);
+/* With graph mode on, swr_draw_batch captures its kernel sequence in a CUDA graph the first
+ * time a batch layout (item count, sizes, shaders, modes) is seen and replays it for later
+ * batches with the same layout; uniforms and buffer pointers are refreshed on every call. */
+int swr_set_graph_mode(swr_context* ctx, int on);
+
 /* Wait for the stream, report and reset the accumulated status. */
 int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
 /* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels. */

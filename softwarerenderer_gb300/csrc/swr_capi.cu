@@ -78,7 +78,8 @@ struct swr_context {
   swr::Buffer draws, targets, draw_vbase, draw_bbase, target_tile_base;
   swr::Buffer ptv, clipv, clip_table, clip_slot, tri_flags, batch_counts, batch_base;
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
-  swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start;
+  swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
+  bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
   // tracing: CUDA events at the stage boundaries of every draw since the last
@@ -87,20 +88,33 @@ struct swr_context {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;  // events recorded (multiple of 6 after a complete draw)
   uint64_t launches = 0;  // kernels launched since the last swr_finish
+  // batched submissions: pinned staging of the descriptor arrays, and the CUDA graph of
+  // the last batch layout
+  unsigned char* stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaEvent_t stage_read = nullptr;  // recorded after the staging copies of the last batch
+  bool stage_pending = false;
+  bool graph_mode = false;
+  bool capturing = false;
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap_stream = nullptr;  // graphs are recorded here, then launched on the caller's stream
+  uint64_t gsig = 0;
+  uint64_t glaunches = 0;  // kernels per replay of the cached graph
 };
 
 namespace {
 
 using namespace swr;
 
-int cuda_err(cudaError_t e) {
+int cuda_err_at(cudaError_t e, int line) {
   if (e == cudaSuccess) return SWR_OK;
-  fprintf(stderr, "swr_gb300: CUDA error %s\n", cudaGetErrorString(e));
+  fprintf(stderr, "swr_gb300: CUDA error %s (swr_capi.cu:%d)\n", cudaGetErrorString(e), line);
   return e == cudaErrorMemoryAllocation ? SWR_ENOMEM : SWR_ECUDA;
 }
+#define cuda_err(e) cuda_err_at((e), __LINE__)
 
 void mark(swr_context* c, int i, cudaStream_t s) {
-  if (!c->profiling) return;
+  if (!c->profiling || c->capturing) return;
   if (i == 0) c->ev_used = (c->ev_used + 5) / 6 * 6;  // start a new sextuple
   const size_t k = c->ev_used;
   if (k >= c->ev_pool.size()) {
@@ -190,7 +204,7 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
 // offsets, k_fill_bins scatters primitive ids into their cells, k_sort_cells restores the
 // primitive order inside each cell; a tile's bin is then its cells' contiguous range.
 int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int vs_a, int vs_p,
-                 uint32_t ntiles, cudaStream_t s) {
+                 uint32_t ntiles, cudaStream_t s, int ntargets = 1) {
   uint32_t* st = c->status.as<uint32_t>();
   const uint32_t ncells = ntiles * SWR_SEGS;
   int seg_shift = 0;
@@ -236,7 +250,8 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.draws = c->draws.as<SwrDrawDesc>();
   ra.targets = c->targets.as<SwrTargetDesc>();
   ra.target_tile_base = c->target_tile_base.as<uint32_t>();
-  ra.ntargets = 1;
+  ra.ntargets = ntargets;
+  ra.draw_prim_base = c->use_draw_pbase ? c->draw_pbase.as<uint32_t>() : nullptr;
   ra.status_w = st;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
@@ -363,6 +378,10 @@ int swr_destroy(swr_context* c) {
   if (!c) return SWR_EINVAL;
   if (c->status_host) cudaFreeHost(c->status_host);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+  if (c->stage_read) cudaEventDestroy(c->stage_read);
+  if (c->stage) cudaFreeHost(c->stage);
   delete c;
   return SWR_OK;
 }
@@ -481,10 +500,12 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   aa.batch_base = c->batch_base.as<uint32_t>();
   aa.tris = c->tris.as<uint4>();
   aa.lp_refs = c->lp_refs.as<uint2>();
+  aa.draw_prim_base = nullptr;  // a single draw numbers its primitives from 0
   aa.status = st;
   aa.cap_clip_slots = c->cap_clip_slots;
   aa.cap_clip_verts = c->cap_clip_verts;
   aa.cap_prims = c->cap_prims;
+  c->use_draw_pbase = false;
   if (mode == SWR_DRAW_TRIANGLE) {
     vs->assemble_count(aa, nbatches, s);
     vs->assemble_emit(aa, nbatches, s);  // derives batch bases and the primitive count itself
@@ -540,6 +561,218 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   c->last_ntiles = ntiles;
   if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, T, s);
   return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s);
+}
+
+int swr_set_graph_mode(swr_context* c, int on) {
+  if (!c) return SWR_EINVAL;
+  c->graph_mode = on != 0;
+  return SWR_OK;
+}
+
+int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stream) {
+  if (!c || !items || n <= 0) return SWR_EINVAL;
+  const VsOps* vs = vs_ops(items[0].vs_id);
+  const PsOps* ps = ps_ops(items[0].ps_id);
+  if (!vs || !ps) return SWR_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<SwrDrawDesc> D(n);
+  std::vector<SwrTargetDesc> T;
+  std::vector<const void*> tcolor;
+  std::vector<uint32_t> vbase(n), bbase(n), tbase;
+  uint64_t V = 0, P = 0, B = 0, NT = 0, PIX = 0;
+  uint64_t sig = 1469598103934665603ull;
+  auto mix = [&](uint64_t x) { sig = (sig ^ x) * 1099511628211ull; };
+  for (int i = 0; i < n; ++i) {
+    const swr_draw_item& it = items[i];
+    if (it.vs_id != items[0].vs_id || it.ps_id != items[0].ps_id || !it.uniforms) return SWR_EINVAL;
+    if (it.cull_mode < 0 || it.cull_mode > 2 || it.raster_mode < 0 || it.raster_mode > 2) return SWR_EINVAL;
+    if (it.count % 3 || (it.count && !it.indices)) return SWR_EINVAL;
+    const SwrUniforms& u = *it.uniforms;
+    if (u.width <= 0 || u.height <= 0 || !u.color) return SWR_EINVAL;
+    uint64_t nv = ~0ull;
+    for (int a = 0; a < vs->attribs; ++a) {
+      const uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
+      if (!it.attrib[a] || it.attrib_stride[a] <= 0 || it.attrib_bytes[a] == 0) return SWR_EINVAL;
+      const uint64_t k = it.attrib_bytes[a] >= elem ? (it.attrib_bytes[a] - elem) / (uint64_t)it.attrib_stride[a] + 1 : 0;
+      nv = k < nv ? k : nv;
+    }
+    if (vs->attribs == 0) nv = 0;
+    // target: shared with an earlier item drawing into the same colour buffer
+    int t = -1;
+    for (size_t j = 0; j < tcolor.size(); ++j)
+      if (tcolor[j] == u.color) t = (int)j;
+    if (t >= 0 && (T[t].width != u.width || T[t].height != u.height)) return SWR_EINVAL;
+    if (t < 0) {
+      SwrTargetDesc td;
+      memset(&td, 0, sizeof(td));
+      td.width = u.width;
+      td.height = u.height;
+      td.tiles_x = (u.width + c->tile - 1) / c->tile;
+      td.tiles_y = (u.height + c->tile - 1) / c->tile;
+      td.tile_base = (uint32_t)NT;
+      td.pixel_base = (uint32_t)PIX;
+      td.first_draw = i;
+      NT += (uint64_t)td.tiles_x * (uint64_t)td.tiles_y;
+      PIX += (uint64_t)u.width * (uint64_t)u.height;
+      t = (int)T.size();
+      T.push_back(td);
+      tcolor.push_back(u.color);
+      tbase.push_back(td.tile_base);
+    }
+    SwrDrawDesc& d = D[i];
+    memset(&d, 0, sizeof(d));
+    for (int a = 0; a < 8; ++a) {
+      d.attrib[a] = it.attrib[a];
+      d.attrib_stride[a] = it.attrib_stride[a];
+    }
+    d.indices = it.indices;
+    d.nidx = (uint32_t)it.count;
+    d.nverts = (uint32_t)nv;
+    d.nprims = (uint32_t)(it.count / 3);
+    d.vbase = (uint32_t)V;
+    d.pbase = (uint32_t)P;
+    d.bbase = (uint32_t)B;
+    d.target = t;
+    d.draw_mode = SWR_DRAW_TRIANGLE;
+    d.cull = it.cull_mode;
+    d.raster_mode = it.raster_mode;
+    d.vp_px = (float)it.viewport[2] / 2.0f;
+    d.vp_py = (float)it.viewport[3] / 2.0f;
+    d.vp_ox = (float)it.viewport[0] + d.vp_px;
+    d.vp_oy = (float)it.viewport[1] + d.vp_py;
+    d.dn = it.depth_range[0];
+    d.df = it.depth_range[1];
+    d.sc_minx = it.scissor[0];
+    d.sc_miny = it.scissor[1];
+    d.sc_maxx = it.scissor[0] + it.scissor[2];
+    d.sc_maxy = it.scissor[1] + it.scissor[3];
+    d.u = u;
+    vbase[i] = (uint32_t)V;
+    bbase[i] = (uint32_t)B;
+    V += nv;
+    P += d.nprims;
+    B += (d.nprims + SWR_BATCH_PRIMS - 1) / SWR_BATCH_PRIMS;
+    mix(nv); mix(d.nprims); mix((uint64_t)t); mix((uint64_t)u.width << 32 | (uint32_t)u.height);
+    mix((uint64_t)it.raster_mode << 8 | (uint64_t)it.cull_mode);
+  }
+  if (V >= 0x7fffffffull || P >= 0x7fffffffull || NT >= 0x7fffffffull / SWR_SEGS || PIX >= 0xffffffffull)
+    return SWR_EINVAL;
+  const int ntg = (int)T.size();
+  int rc = ensure_capacity(c, (uint32_t)V, vs->S, (uint32_t)P, (uint32_t)B, (uint32_t)NT,
+                           ps->R > ps->lp_R ? ps->R : ps->lp_R);
+  if (rc) return rc;
+  bool ok = c->draws.ensure(sizeof(SwrDrawDesc) * n) && c->targets.ensure(sizeof(SwrTargetDesc) * ntg) &&
+            c->draw_vbase.ensure(4 * n + 16) && c->draw_bbase.ensure(4 * n + 16) && c->draw_pbase.ensure(4 * n + 16) &&
+            c->target_tile_base.ensure(4 * ntg + 16);
+  if (!ok) return SWR_ENOMEM;
+  // pinned staging; wait until the previous batch's copies have read it
+  const size_t bytes = sizeof(SwrDrawDesc) * n + sizeof(SwrTargetDesc) * ntg + 4 * (2 * n + ntg) + 64;
+  if (c->stage_pending && c->stage_read) {
+    if ((rc = cuda_err(cudaEventSynchronize(c->stage_read)))) return rc;
+    c->stage_pending = false;
+  }
+  if (bytes > c->stage_bytes) {
+    if (c->stage) cudaFreeHost(c->stage);
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+    if ((rc = cuda_err(cudaMallocHost((void**)&c->stage, bytes * 2)))) return rc;
+    c->stage_bytes = bytes * 2;
+  }
+  if (!c->stage_read && (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_read, cudaEventDisableTiming)))) return rc;
+  unsigned char* h = c->stage;
+  const size_t o_d = 0, o_t = o_d + sizeof(SwrDrawDesc) * n, o_vb = o_t + sizeof(SwrTargetDesc) * ntg;
+  const size_t o_bb = o_vb + 4 * n, o_tb = o_bb + 4 * n;
+  memcpy(h + o_d, D.data(), sizeof(SwrDrawDesc) * n);
+  memcpy(h + o_t, T.data(), sizeof(SwrTargetDesc) * ntg);
+  memcpy(h + o_vb, vbase.data(), 4 * n);
+  memcpy(h + o_bb, bbase.data(), 4 * n);
+  memcpy(h + o_tb, tbase.data(), 4 * ntg);
+  mix((uint64_t)vs->S); mix((uint64_t)ps->R); mix((uint64_t)c->tile); mix((uint64_t)n);
+  mix(c->cap_prims); mix(c->cap_pairs); mix(c->cap_clip_slots); mix(c->cap_clip_verts);
+  const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
+                        c->tris.p, c->recs.p, c->tile_count.p, c->keys0.p, c->vals0.p, c->cell_count.p,
+                        c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
+                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->stage};
+  for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
+  if (c->graph_mode && c->gexec && sig == c->gsig) {
+    if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;
+    c->stage_pending = true;
+    c->launches += c->glaunches;
+    return SWR_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  const uint64_t launches0 = c->launches;
+  cudaStream_t launch_stream = s;
+  if (c->graph_mode) {
+    // the caller's stream may be the legacy default stream, which cannot be captured
+    if (!c->cap_stream && (rc = cuda_err(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking))))
+      return rc;
+    s = c->cap_stream;
+    if ((rc = cuda_err(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)))) return rc;
+    c->capturing = true;
+  }
+  int q = SWR_OK;
+  q = q ? q : cuda_err(cudaMemcpyAsync(c->draws.p, h + o_d, sizeof(SwrDrawDesc) * n, cudaMemcpyHostToDevice, s));
+  q = q ? q : cuda_err(cudaMemcpyAsync(c->targets.p, h + o_t, sizeof(SwrTargetDesc) * ntg, cudaMemcpyHostToDevice, s));
+  q = q ? q : cuda_err(cudaMemcpyAsync(c->draw_vbase.p, h + o_vb, 4 * n, cudaMemcpyHostToDevice, s));
+  q = q ? q : cuda_err(cudaMemcpyAsync(c->draw_bbase.p, h + o_bb, 4 * n, cudaMemcpyHostToDevice, s));
+  q = q ? q : cuda_err(cudaMemcpyAsync(c->target_tile_base.p, h + o_tb, 4 * ntg, cudaMemcpyHostToDevice, s));
+  // the host waits on this event before it rewrites the staging area; inside a capture
+  // only an external record becomes a node the host can wait on
+  q = q ? q : cuda_err(c->capturing ? cudaEventRecordWithFlags(c->stage_read, s, cudaEventRecordExternal)
+                                    : cudaEventRecord(c->stage_read, s));
+  q = q ? q : cuda_err(cudaMemsetAsync(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 0, 5 * 4, s));
+  q = q ? q : cuda_err(cudaGetLastError());
+  uint32_t* st = c->status.as<uint32_t>();
+  mark(c, 0, s);
+  vs->vertex(c->draws.as<SwrDrawDesc>(), n, c->draw_vbase.as<uint32_t>(), (uint32_t)V, c->ptv.as<float>(), s);
+  mark(c, 1, s);
+  AssembleArgs aa;
+  memset(&aa, 0, sizeof(aa));
+  aa.draws = c->draws.as<SwrDrawDesc>();
+  aa.ndraws = n;
+  aa.draw_bbase = c->draw_bbase.as<uint32_t>();
+  aa.ptv = c->ptv.as<float>();
+  aa.clipv = c->clipv.as<float>();
+  aa.clip_table = c->clip_table.as<SwrClipEntry>();
+  aa.clip_slot = c->clip_slot.as<uint32_t>();
+  aa.tri_flags = c->tri_flags.as<uint8_t>();
+  aa.batch_counts = c->batch_counts.as<uint2>();
+  aa.batch_base = c->batch_base.as<uint32_t>();
+  aa.tris = c->tris.as<uint4>();
+  aa.lp_refs = c->lp_refs.as<uint2>();
+  aa.draw_prim_base = c->draw_pbase.as<uint32_t>();
+  aa.status = st;
+  aa.cap_clip_slots = c->cap_clip_slots;
+  aa.cap_clip_verts = c->cap_clip_verts;
+  aa.cap_prims = c->cap_prims;
+  c->use_draw_pbase = true;
+  vs->assemble_count(aa, (uint32_t)B, s);
+  vs->assemble_emit(aa, (uint32_t)B, s);
+  mark(c, 2, s);
+  c->launches += (V ? 1 : 0) + (B ? 2 : 0);
+  if (!q) q = cuda_err(cudaGetLastError());
+  rc = raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, (uint32_t)NT, s, ntg);
+  if (q) rc = q;
+  c->use_draw_pbase = false;
+  if (c->graph_mode) {
+    c->capturing = false;
+    const int rc2 = cuda_err(cudaStreamEndCapture(s, &graph));
+    if (rc || rc2) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc ? rc : rc2;
+    }
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    rc = cuda_err(cudaGraphInstantiate(&c->gexec, graph, 0));
+    cudaGraphDestroy(graph);
+    if (rc) return rc;
+    c->gsig = sig;
+    c->glaunches = c->launches - launches0;
+    if ((rc = cuda_err(cudaGraphLaunch(c->gexec, launch_stream)))) return rc;
+  }
+  c->stage_pending = true;
+  return rc;
 }
 
 int swr_finish(swr_context* c, void* stream, swr_stats* stats) {

@@ -211,6 +211,7 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.targets = dt;
   ra.target_tile_base = zeros;
   ra.ntargets = 1;
+  ra.draw_prim_base = nullptr;
   ra.status_w = st;
   ps->raster(ra, ntiles, kTile, s);
   uint32_t h[16];

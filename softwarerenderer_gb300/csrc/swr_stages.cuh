@@ -190,6 +190,7 @@ struct AssembleArgs {
   const uint32_t* batch_base;
   uint4* tris;              // output primitives: v0, v1, v2 references + draw id
   uint2* lp_refs;           // per submitted point / line: endpoint references after clipping
+  uint32_t* draw_prim_base; // per draw: index of its first emitted primitive (optional)
   uint32_t* status;
   uint32_t cap_clip_slots, cap_clip_verts, cap_prims;
 };
@@ -367,6 +368,8 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
   swr_block_exscan(before, tmp, &base);
   const uint2 c0 = g.batch_counts[2 * b], c1 = g.batch_counts[2 * b + 1];
   const uint32_t batch_in = c0.x + c1.x, batch_total = batch_in + c0.y + c1.y;
+  // primitive ids seen by the pixel shader are per draw, as with one drawElements call each
+  if (g.draw_prim_base && b == D.bbase && half == 0 && threadIdx.x == 0) g.draw_prim_base[d] = base;
   // effective order within the batch: every kept input slot (first half, then second),
   // then every extra fan triangle (first half's, then second's)
   const uint32_t in_base = base + (half ? c0.x : 0u);
@@ -873,6 +876,7 @@ struct RasterArgs {
   const SwrTargetDesc* targets;
   const uint32_t* target_tile_base;  // per target, for the tile -> target lookup
   int ntargets;
+  const uint32_t* draw_prim_base;    // per draw first primitive (null: a single draw from 0)
   uint32_t* status_w;
 };
 
@@ -932,6 +936,11 @@ __device__ __forceinline__ uint32_t block_row_bits(const float* r, int flags, in
     i2 = swr_add(i2, r[12]);
   }
   return m;
+}
+
+// Primitive id handed to the pixel shader: the index within its own draw.
+__device__ __forceinline__ int prim_id(const RasterArgs& g, const float* rec, uint32_t p) {
+  return (int)(p - (g.draw_prim_base ? g.draw_prim_base[__float_as_int(rec[1])] : 0u));
 }
 
 // Position (0-63) of the j-th set bit of m (j < popcount(m)).
@@ -1222,7 +1231,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
           int rank = __popcll(m & ((1ull << bit) - 1ull));
           for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
           const int f = (int)sex[k] + rank;
-          PS::apply(st[q], sfz[f], sfc[f], (int)sids[k]);
+          PS::apply(st[q], sfz[f], sfc[f], prim_id(g, r, sids[k]));
           continue;
         }
         const bool blockmode = __float_as_int(r[0]) & 2;
@@ -1247,7 +1256,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
         pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
         if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
         build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
-        PS::drawPixel(pd, (int)sids[k], st[q], g.draws[__float_as_int(r[1])].u);
+        PS::drawPixel(pd, prim_id(g, r, sids[k]), st[q], g.draws[__float_as_int(r[1])].u);
       }
     }
   }

@@ -489,3 +489,77 @@ def scene_digest(scene: Scene) -> str:
                    tuple(float(x) for x in scene.depth_range), tuple(scene.scissor),
                    scene.checker)).encode())
     return h.hexdigest()[:32]
+
+
+# ----------------------------------------------------------------------------
+# config: batched rendering of many meshes, each to its own target
+
+def _deformed_sphere(level: int, ntris: int, rng):
+    """The first `ntris` triangles of an icosphere level, radially deformed by a seeded
+    polynomial (no transcendental functions), with normals from the deformed positions'
+    face-normal average and planar uv."""
+    p, f = icosphere(level)
+    f = f[:ntris]
+    c = rng.random(6) * 0.4 - 0.2
+    x, y, z = p[:, 0], p[:, 1], p[:, 2]
+    r = 1.0 + c[0] * x * y + c[1] * y * z + c[2] * z * x + c[3] * x * x + c[4] * y * y * y + c[5] * z
+    q = p * r[:, None]
+    a, b, cc = q[f[:, 0]], q[f[:, 1]], q[f[:, 2]]
+    fn = np.cross(b - a, cc - a)
+    nrm = np.zeros_like(q)
+    for k in range(3):
+        np.add.at(nrm, f[:, k], fn)
+    ln = np.sqrt(nrm[:, 0] * nrm[:, 0] + nrm[:, 1] * nrm[:, 1] + nrm[:, 2] * nrm[:, 2])
+    ln[ln == 0] = 1.0
+    nrm = nrm / ln[:, None]
+    pn = np.concatenate([q, nrm], axis=1).astype(np.float32)
+    uv = np.stack([(p[:, 0] + 1.0) * 0.5, (p[:, 2] + 1.0) * 0.5], 1).astype(np.float32)
+    return pn, uv, f.reshape(-1).astype(np.int32)
+
+
+def _mesh_texture(rng, size=512):
+    y, x = np.mgrid[0:size, 0:size].astype(np.uint32)
+    sq = int(rng.integers(8, 64))
+    col = rng.integers(0, 256, (2, 3)).astype(np.uint32)
+    on = ((x // sq + y // sq) & 1).astype(bool)
+    r = np.where(on, col[0, 0], col[1, 0]) ^ (x & 15)
+    g = np.where(on, col[0, 1], col[1, 1]) ^ (y & 15)
+    b = np.where(on, col[0, 2], col[1, 2])
+    return (r | (g << 8) | (b << 16) | (np.uint32(255) << 24)).astype(np.uint32)
+
+
+def batch_scenes(n: int = 256, seed: int = 4, max_tris: int = 200_000, min_tris: int = 100,
+                 sides=(256, 512, 768, 1024), texture_size: int = 512):
+    """`n` meshes for one batched submission: triangle counts piecewise-log-uniform in
+    [min_tris, max_tris] (octave + linear, truncating the index list of the icosphere level
+    that has enough triangles), target side drawn from `sides`, own camera and RGBA8 texture.
+    Block mode, CullMode CW, Lambert x nearest texture."""
+    rng = np.random.default_rng(seed)
+    lo, hi = float(min_tris), float(max_tris)
+    out = []
+    for i in range(n):
+        # log-uniform via octave + linear fraction (exact powers of two)
+        span = hi / lo
+        octs = int(np.floor(np.log2(span)))  # deterministic: exact for these integer bounds
+        while True:
+            e = int(rng.integers(0, octs + 1))
+            t = lo * float(np.ldexp(1.0, e)) * (1.0 + float(rng.random()))
+            if t <= hi:
+                break
+        ntris = max(1, int(t))
+        level = 0
+        while 20 * 4 ** level < ntris:
+            level += 1
+        pn, uv, idx = _deformed_sphere(level, ntris, rng)
+        side = int(sides[int(rng.integers(0, len(sides)))])
+        d = 2.4 + 1.6 * float(rng.random())
+        mvp = mat_to_f32(_matmul4(perspective(1.0, 0.1, 100.0), _matmul4(translate(0.0, 0.0, -d),
+                                                                          random_rotation(rng))))
+        l = normalized([float(rng.random()) - 0.5, float(rng.random()) - 0.5, 1.0])
+        out.append(Scene(name=f"batch{i}[{ntris}t,{side}px]", vs=VS.POS_NRM_UV, ps=PS.LAMBERT_TEX,
+                         width=side, height=side, cull=CullMode.CW, raster=RasterMode.Block,
+                         viewport=(0, 0, side, side), scissor=(0, 0, side, side),
+                         attribs=[(pn, 24), (uv, 8)], indices=idx, mvp=mvp,
+                         light=np.array([l[0], l[1], l[2], 0.2], np.float32),
+                         texture=_mesh_texture(rng, texture_size)))
+    return out

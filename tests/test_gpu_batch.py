@@ -1,0 +1,51 @@
+"""Batched rendering (swr_draw_batch) against the CPU oracle, item by item.
+
+A batch is one pass of the pipeline over all items; each item's target must equal what
+the reference renders for that item alone (bit for bit), including items that share a
+target (drawn in item order) and replays of the captured CUDA graph.
+"""
+import numpy as np
+import pytest
+
+from softwarerenderer_gb300 import scenes
+
+from .parity import diff, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_batch(n=10, seed=41):
+    return scenes.batch_scenes(n, seed=seed, max_tris=3000, min_tris=20, sides=(48, 64, 96, 128),
+                               texture_size=64)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_matches_oracle(gpu_lib, port, graph):
+    from softwarerenderer_gb300.batch import BatchRenderer
+    scs = _small_batch()
+    br = BatchRenderer(scs, aux=True, graph=graph)
+    for rep in range(2):  # second pass replays the graph
+        br.clear()
+        br.draw()
+        for sc, tg in zip(scs, br.targets):
+            ref, _ = oracle_render(port, sc)
+            assert not diff(ref, tg.to_host()), (rep, sc.name)
+
+
+def test_batch_shared_target_in_item_order(gpu_lib, port):
+    """Items drawing into one colour buffer meet in one bin per tile, in item order."""
+    from softwarerenderer_gb300.batch import BatchRenderer
+    from softwarerenderer_gb300.device import DeviceTarget
+    base = scenes.batch_scenes(4, seed=7, max_tris=2000, min_tris=200, sides=(96,), texture_size=64)
+    shared = DeviceTarget(base[0], aux=True)
+    br = BatchRenderer(base, aux=True, graph=False, targets=[shared] * len(base))
+    br.clear()
+    br.draw()
+    # oracle: the same items drawn one after another into one host target
+    t = scenes.Target(base[0])
+    for sc in base:
+        port.draw(sc, t)
+    got = shared.to_host()
+    # primitive ids restart per drawElements call, in the oracle and in the batch
+    for k in ("color", "depth", "frag_count", "winner"):
+        assert np.asarray(t.arrays()[k]).tobytes() == np.asarray(got[k]).tobytes(), k
