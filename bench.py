@@ -190,6 +190,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--tile", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     args = ap.parse_args()
     assert args.warmup >= 3, "at least 3 warm-up steps"
 
@@ -295,6 +296,9 @@ def main():
 
     # e2e through the public API with host buffers
     e2e = run_e2e(ds, tg, sc, poses, args, torch)
+    batched = None
+    if not args.no_batch:
+        batched = run_batched(torch)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -314,10 +318,51 @@ def main():
                 "stage_ms_per_frame": {k: round(v / args.steps, 4) for k, v in stages.items()},
                 "gpu_launches": int(st["launches"]),
                 "roofline": roofline, "frame_roofline": frame_roof,
-                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb}
+                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def run_batched(torch, n=256, steps=10):
+    """Batched views/s: 256 seeded meshes (100 to 200k triangles each, piecewise-log-uniform;
+    targets 256..1024 px square; own camera and 512x512 RGBA8 texture) rendered by one
+    swr_draw_batch per step (configuration from the autotuner, CUDA graph replay) against
+    the same views as 256 separate drawElements calls per step.  Targets total ~1 GB, larger
+    than L2."""
+    from softwarerenderer_gb300 import autotune, scenes
+    from softwarerenderer_gb300.batch import BatchRenderer
+    scs = scenes.batch_scenes(n)
+    best = autotune.tune(scs)
+    br = BatchRenderer(scs, tile=best["tile"], graph=best["graph"], pooled=True)
+    res = {"n_views": n, "triangles_per_step": int(sum(len(x.indices) // 3 for x in scs)),
+           "pixels_per_step": int(sum(x.width * x.height for x in scs)), "autotune": best}
+    for mode in ("batch", "loop"):
+        fn = br.draw if mode == "batch" else br.draw_loop
+        for _ in range(3):
+            br.clear()
+            fn()
+        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s0.record()
+        for _ in range(steps):
+            br.clear()
+            fn(sync=False)
+        e0.record()
+        torch.cuda.synchronize()
+        if mode == "batch":
+            rc, st = br.ctx.finish()
+            assert rc == 0, rc
+        else:
+            for ds in br.dev:
+                rc, _ = ds.rast.ctx.finish()
+                assert rc == 0, rc
+        ms = s0.elapsed_time(e0) / steps
+        res[f"{mode}_ms_per_step"] = round(ms, 4)
+        res[f"{mode}_views_per_s"] = round(n / (ms / 1e3), 1)
+    res["speedup_vs_loop"] = round(res["batch_views_per_s"] / res["loop_views_per_s"], 3)
+    res["batch_mtris_per_s"] = round(res["triangles_per_step"] / (res["batch_ms_per_step"] / 1e3) / 1e6, 1)
+    return res
 
 
 def run_e2e(ds, tg, sc, poses, args, torch):

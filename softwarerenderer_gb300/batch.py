@@ -34,8 +34,41 @@ class SwrDrawItem(ctypes.Structure):
 assert ctypes.sizeof(SwrDrawItem) == 240
 
 
+class _PooledTarget:
+    """A render target whose colour and depth are views into pooled buffers."""
+
+    def __init__(self, color, depth):
+        self.color, self.depth = color, depth
+        self.frag_count = self.winner = None
+
+    def to_host(self):
+        return {"color": self.color.cpu().numpy().view("uint32"), "depth": self.depth.cpu().numpy()}
+
+
+class TargetPool:
+    """One colour and one depth allocation sliced into per-scene targets (RGBA8 shaders),
+    so a whole batch is cleared by two fills."""
+
+    def __init__(self, scenes, clear_color=0, clear_depth=float("inf")):
+        sizes = [sc.width * sc.height for sc in scenes]
+        total = sum(sizes)
+        self.color = torch.full((total,), int(clear_color), dtype=torch.int32, device="cuda")
+        self.depth = torch.full((total,), clear_depth, dtype=torch.float32, device="cuda")
+        self.clear_color, self.clear_depth = clear_color, clear_depth
+        self.targets = []
+        off = 0
+        for sc, n in zip(scenes, sizes):
+            self.targets.append(_PooledTarget(self.color[off:off + n].view(sc.height, sc.width),
+                                              self.depth[off:off + n].view(sc.height, sc.width)))
+            off += n
+
+    def clear(self):
+        self.color.fill_(self.clear_color)
+        self.depth.fill_(self.clear_depth)
+
+
 class BatchRenderer:
-    def __init__(self, scenes, aux=False, tile=16, graph=True, targets=None):
+    def __init__(self, scenes, aux=False, tile=16, graph=True, targets=None, pooled=False):
         self.ctx = Context()
         L = self.ctx.L
         L.swr_draw_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(SwrDrawItem), ctypes.c_int, ctypes.c_void_p]
@@ -47,7 +80,11 @@ class BatchRenderer:
         self.scenes = scenes
         self.dev = [DeviceScene(sc, tile=tile) for sc in scenes]
         # by default one target per scene; `targets` may map scenes onto shared targets
-        self.targets = targets if targets is not None else [DeviceTarget(sc, aux=aux) for sc in scenes]
+        self.pool = TargetPool(scenes) if pooled and targets is None else None
+        if self.pool is not None:
+            self.targets = self.pool.targets
+        else:
+            self.targets = targets if targets is not None else [DeviceTarget(sc, aux=aux) for sc in scenes]
         self.items = (SwrDrawItem * len(scenes))()
         self.uniforms = []
         self._fill()
@@ -73,6 +110,9 @@ class BatchRenderer:
             it.uniforms = ctypes.pointer(u)
 
     def clear(self):
+        if self.pool is not None:
+            self.pool.clear()
+            return
         for tg in self.targets:
             tg.clear()
 
