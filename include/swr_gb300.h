@@ -115,6 +115,8 @@ typedef struct swr_draw_item {
   const uint32_t* indices;
   uint64_t count;
   const struct SwrUniforms* uniforms;
+  int32_t* prim_src;           /* optional primitive-source output, see swr_set_primitive_source */
+  uint64_t prim_src_capacity;
 } swr_draw_item;
 
 int swr_draw_batch(swr_context* ctx, const swr_draw_item* items, int n, void* stream);
@@ -136,6 +138,57 @@ const char* swr_status_string(int status);
  * setup, binning, tile raster. */
 int swr_set_profiling(swr_context* ctx, int on);
 int swr_stage_times(swr_context* ctx, float* ms5);
+
+/* Primitive sources (no reference counterpart; needed by swr_backward).  While set, each
+ * triangle swr_draw_elements call writes out[k] = t, the source triangle (indices
+ * [3t, 3t + 3) of its index list) of its k-th rasterized primitive -- k being the id the
+ * pixel shaders see and SwrUniforms.winner records (the rasterizer's primitive numbering,
+ * VertexProcessor.cpp:281-317 then Rasterizer.h:134-141).  A triangle that clipping splits
+ * yields several primitives with one source.  At most `capacity` entries are written; a
+ * draw with more primitives makes swr_finish return SWR_EINVAL.  NULL turns it off.
+ * (swr_draw_item.prim_src is the same output for one item of a batch.) */
+int swr_set_primitive_source(swr_context* ctx, int32_t* out, uint64_t capacity);
+
+/* Differentiable rendering (no reference counterpart: the reference renders forward only).
+ * The forward is an ordinary draw with vertex shader SWR_VS_POS_RGB_UV and pixel shader
+ * SWR_PS_DIFF (colour = interpolated vertex rgb * bilinear RGBA32F texel) that records the
+ * winner buffer and the primitive sources.  swr_backward then returns the gradients of a
+ * scalar image loss L with respect to the vertex records {x, y, z, r, g, b, u, v} and the
+ * texels, with visibility held fixed (each pixel keeps the primitive that won it); the
+ * position gradient flows through the perspective-correct barycentrics, which each tile
+ * recomputes from the clip-space vertices (nothing per pixel is stored by the forward). */
+typedef struct swr_grad_view {
+  float mvp[16];            /* the view's SwrUniforms.mvp */
+  int32_t viewport[4];      /* the view's viewport: x, y, width, height */
+  int32_t width, height;    /* render target size; row pitch == width */
+  const int32_t* winner;    /* forward output: per pixel primitive id, -1 = not covered */
+  const int32_t* prim_src;  /* forward output: source triangle per primitive id */
+  uint64_t nprims;          /* valid entries of prim_src */
+  const float* grad_color;  /* dL/d(colour), RGBA32F per pixel; NULL selects the fused L2 loss: */
+  const float* color;       /*   forward image, RGBA32F per pixel */
+  const float* target;      /*   target image, RGBA32F per pixel */
+  float loss_scale;         /*   L = loss_scale * sum over pixels and channels of (color - target)^2 */
+  int32_t _pad;
+} swr_grad_view;
+
+typedef struct swr_backward_args {
+  const float* vertices;    /* nverts records of 8 floats (stride 32 B, 16-byte aligned) */
+  uint64_t nverts;
+  const uint32_t* indices;  /* the forward's triangle list */
+  uint64_t count;
+  const float* texture;     /* RGBA32F texels, tex_h rows of tex_w (16-byte aligned) */
+  int32_t tex_w, tex_h;
+  float* grad_vertices;     /* += dL/d(vertex record): nverts x 8 floats (16-byte aligned) */
+  float* grad_texture;      /* += dL/d(texel): tex_h x tex_w x 4 floats (16-byte aligned) */
+  double* loss;             /* fused loss only: += L (may be NULL) */
+} swr_backward_args;
+
+/* Queues the backward of `nviews` views on `stream`; gradients accumulate (clear them
+ * first).  Ids beyond nprims / the triangle count / the vertex count are skipped and make
+ * swr_finish return SWR_EINDEX.  Float atomics make the summation order (not the terms)
+ * vary from run to run. */
+int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad_view* views, int nviews,
+                 void* stream);
 
 /* Allocation-free triangle-list draw.  No counterpart in the reference (whose CPU
  * rasterizer needs no device scratch).  It is swr_draw_list(SWR_DRAW_TRIANGLE, ...) for

@@ -38,7 +38,22 @@ class OracleDraw(ctypes.Structure):
         ("uniforms", ctypes.POINTER(SwrUniforms)),
         ("threads", ctypes.c_int32),
         ("_pad", ctypes.c_int32),
+        ("prim_src", ctypes.c_void_p),
+        ("prim_src_cap", ctypes.c_uint64),
     ]
+
+
+class OracleDiffScene(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("nverts", ctypes.c_uint64),
+                ("indices", ctypes.c_void_p), ("count", ctypes.c_uint64),
+                ("texture", ctypes.c_void_p), ("tex_w", ctypes.c_int32), ("tex_h", ctypes.c_int32)]
+
+
+class OracleDiffView(ctypes.Structure):
+    _fields_ = [("mvp", ctypes.c_float * 16), ("viewport", ctypes.c_int32 * 4),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("winner", ctypes.c_void_p), ("prim_src", ctypes.c_void_p), ("nprims", ctypes.c_uint64),
+                ("grad_color", ctypes.c_void_p), ("target", ctypes.c_void_p)]
 
 
 class OracleStats(ctypes.Structure):
@@ -66,6 +81,14 @@ def load(which="port"):
         lib.oracle_draw.restype = ctypes.c_int
         lib.oracle_fold.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int]
         lib.oracle_fold.restype = ctypes.c_float
+        if hasattr(lib, "oracle_diff_eval"):
+            lib.oracle_diff_eval.argtypes = [ctypes.POINTER(OracleDiffScene), ctypes.POINTER(OracleDiffView),
+                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            lib.oracle_diff_eval.restype = ctypes.c_int
+            lib.oracle_diff_fd.argtypes = [ctypes.POINTER(OracleDiffScene), ctypes.POINTER(OracleDiffView),
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
+            lib.oracle_diff_fd.restype = ctypes.c_int
         if hasattr(lib, "oracle_fold_selftest"):
             lib.oracle_fold_selftest.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
             lib.oracle_fold_selftest.restype = ctypes.c_uint64
@@ -85,8 +108,9 @@ class Oracle:
     def fold(self, v, a, k):
         return self.lib.oracle_fold(v, a, k)
 
-    def draw(self, scene, target, threads=0):
-        """Render `scene` into `target` (numpy buffers, modified in place); returns stats."""
+    def draw(self, scene, target, threads=0, prim_src=None):
+        """Render `scene` into `target` (numpy buffers, modified in place); returns stats.
+        `prim_src` (int32 array, port only) receives the source triangle of every primitive."""
         keep = []
         tex = scene.texture
         if tex is not None:
@@ -119,9 +143,71 @@ class Oracle:
             d.raster_vertices = rv.ctypes.data
         d.uniforms = ctypes.pointer(u)
         d.threads = int(threads)
+        if prim_src is not None:
+            assert prim_src.dtype == np.int32 and prim_src.flags.c_contiguous
+            d.prim_src = prim_src.ctypes.data
+            d.prim_src_cap = int(prim_src.size)
         st = OracleStats()
         rc = self.lib.oracle_draw(ctypes.byref(d), ctypes.byref(st))
         if rc != 0:
             raise ValueError(f"oracle_draw rejected the draw (status {rc})")
         return {"fragments": st.fragments, "outside": st.outside,
                 "primitives": st.primitives, "batches": st.batches}
+
+    # --- differentiable rendering reference (port only) -------------------------------
+
+    def _diff_args(self, problem, views):
+        """problem: softwarerenderer_gb300.scenes.DiffProblem; views: list of dicts with
+        mvp, winner, prim_src, and grad_color and/or target (numpy)."""
+        keep = []
+        vd = np.ascontiguousarray(problem.vertices, dtype=np.float64)
+        td = np.ascontiguousarray(problem.texture, dtype=np.float64)
+        idx = np.ascontiguousarray(problem.indices, dtype=np.int32)
+        keep += [vd, td, idx]
+        sc = OracleDiffScene(vd.ctypes.data, vd.shape[0], idx.ctypes.data, idx.size, td.ctypes.data,
+                             td.shape[1], td.shape[0])
+        arr = (OracleDiffView * len(views))()
+        for k, v in enumerate(views):
+            o = arr[k]
+            m = np.ascontiguousarray(v["mvp"], dtype=np.float32).reshape(16)
+            for i in range(16):
+                o.mvp[i] = float(m[i])
+            for i in range(4):
+                o.viewport[i] = int(problem.viewport[i])
+            o.width, o.height = problem.width, problem.height
+            w = np.ascontiguousarray(v["winner"], dtype=np.int32)
+            ps = np.ascontiguousarray(v["prim_src"], dtype=np.int32)
+            keep += [w, ps]
+            o.winner, o.prim_src, o.nprims = w.ctypes.data, ps.ctypes.data, ps.size
+            for name in ("grad_color", "target"):
+                a = v.get(name)
+                if a is not None:
+                    a = np.ascontiguousarray(a, dtype=np.float32)
+                    keep.append(a)
+                    setattr(o, name, a.ctypes.data)
+        return sc, arr, keep
+
+    def diff_eval(self, problem, views, grads=True):
+        """(loss, grad_vertices (V, 8), grad_texture (T, T, 4)) in double."""
+        sc, arr, keep = self._diff_args(problem, views)
+        loss = ctypes.c_double(0.0)
+        gv = np.zeros(problem.vertices.shape, np.float64) if grads else None
+        gt = np.zeros(problem.texture.shape, np.float64) if grads else None
+        rc = self.lib.oracle_diff_eval(ctypes.byref(sc), arr, len(views), ctypes.addressof(loss),
+                                       _ptr(gv), _ptr(gt))
+        if rc != 0:
+            raise ValueError(f"oracle_diff_eval failed (status {rc})")
+        return loss.value, gv, gt
+
+    def diff_fd(self, problem, views, kind, index, h=1e-3, threads=0):
+        """Central differences of the fixed-visibility L2 loss for parameters (kind, index):
+        kind 0 = vertex-record component (8 * vertex + c), 1 = texel component (4 * texel + c)."""
+        sc, arr, keep = self._diff_args(problem, views)
+        kind = np.ascontiguousarray(kind, dtype=np.int32)
+        index = np.ascontiguousarray(index, dtype=np.uint64)
+        out = np.zeros(kind.size, np.float64)
+        rc = self.lib.oracle_diff_fd(ctypes.byref(sc), arr, len(views), kind.ctypes.data, index.ctypes.data,
+                                     kind.size, float(h), out.ctypes.data, int(threads))
+        if rc != 0:
+            raise ValueError(f"oracle_diff_fd failed (status {rc})")
+        return out

@@ -30,6 +30,10 @@ typedef struct OracleDraw {
   const SwrUniforms* uniforms;
   int32_t threads;           /* OpenMP threads for the port (0 = runtime default) */
   int32_t _pad;
+  /* Port only (triangles through drawElements): prim_src[k] = source triangle of the k-th
+   * primitive handed to the rasterizer; at most prim_src_cap entries are written. */
+  int32_t* prim_src;
+  uint64_t prim_src_cap;
 } OracleDraw;
 
 typedef struct OracleStats {
@@ -41,6 +45,43 @@ typedef struct OracleStats {
 
 /* Returns 0 on success, non-zero on invalid input. */
 int oracle_draw(const OracleDraw* d, OracleStats* st);
+
+/* Differentiable rendering reference (port only, oracle/port/swr_diff.cpp), in double.
+ * Scene: vertex records {x, y, z, r, g, b, u, v} (the SWR_VS_POS_RGB_UV stream) and an
+ * RGBA32F texture, widened to double by the caller.  A view is one forward draw with
+ * PsDiff: its mvp, viewport and target size, its winner buffer and primitive-source map
+ * (visibility, held fixed), the target image of the L2 loss and/or dL/d(colour). */
+typedef struct OracleDiffScene {
+  const double* vertices;  /* nverts x 8 */
+  uint64_t nverts;
+  const int32_t* indices;  /* triangle list */
+  uint64_t count;
+  const double* texture;   /* tex_h x tex_w x 4 */
+  int32_t tex_w, tex_h;
+} OracleDiffScene;
+
+typedef struct OracleDiffView {
+  float mvp[16];
+  int32_t viewport[4];
+  int32_t width, height;
+  const int32_t* winner;     /* per pixel primitive id, -1 none */
+  const int32_t* prim_src;   /* per primitive id its source triangle */
+  uint64_t nprims;
+  const float* grad_color;   /* dL/d(colour) per pixel (RGBA), or NULL: 2 (colour - target) */
+  const float* target;       /* RGBA per pixel, or NULL (then grad_color is required) */
+} OracleDiffView;
+
+/* loss (may be NULL) = sum over covered pixels and channels of (colour - target)^2 with the
+ * colour recomputed at fixed visibility; grad_vertices (nverts x 8) and grad_texture
+ * (tex_h x tex_w x 4), each may be NULL, receive += dL/d(parameter).  Returns 0, 1 for
+ * invalid arguments, 2 for a winner or source id beyond the given counts. */
+int oracle_diff_eval(const OracleDiffScene* s, const OracleDiffView* views, int nviews, double* loss,
+                     double* grad_vertices, double* grad_texture);
+/* Central differences (L(p + h) - L(p - h)) / 2h of that loss for n parameters:
+ * kind 0 = vertex-record component index (8 * vertex + component), kind 1 = texel
+ * component (4 * texel + channel).  OpenMP over parameters (threads 0 = default). */
+int oracle_diff_fd(const OracleDiffScene* s, const OracleDiffView* views, int nviews, const int32_t* kind,
+                   const uint64_t* index, int n, double h, double* out, int threads);
 /* swr_fold exposed for the tests of the fast-forward. */
 float oracle_fold(float v, float a, int k);
 /* Randomized comparison of swr_fold with serial stepping; returns the mismatch count. */

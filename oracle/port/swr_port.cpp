@@ -104,6 +104,9 @@ struct Pix {
 
 struct Counters {
   uint64_t frags = 0, outside = 0, prims = 0, batches = 0;
+  int32_t* prim_src = nullptr;  // optional: source triangle per primitive id
+  uint64_t prim_src_cap = 0;
+  bool src_overflow = false;
 };
 
 // Rasterizer restatement (Rasterizer.h:52-446) for pixel shader PS.
@@ -427,6 +430,7 @@ struct VP {
   int draw_mode;
   std::vector<Vtx> verts;
   std::vector<int> idx;
+  std::vector<int> src;  // per triangle of idx: its source triangle in the draw's index list
   std::vector<int> mask;
   std::vector<char> done;
   const void* raster;
@@ -482,6 +486,7 @@ struct VP {
         idx.push_back(poly[0]);
         idx.push_back(poly[k - 1]);
         idx.push_back(poly[k]);
+        src.push_back(src[i / 3]);
       }
     }
   }
@@ -570,6 +575,16 @@ struct VP {
     else clip_triangles();
     transform();
     if (draw_mode == 2) cull_triangles();
+    if (draw_mode == 2 && cnt->prim_src) {
+      // the rasterizer numbers the surviving triangles in idx order
+      uint64_t k = cnt->prims;
+      for (size_t i = 0; i + 3 <= idx.size(); i += 3) {
+        if (idx[i] == -1) continue;
+        if (k < cnt->prim_src_cap) cnt->prim_src[k] = src[i / 3];
+        else cnt->src_overflow = true;
+        ++k;
+      }
+    }
     list(raster, draw_mode, verts.data(), idx.data(), idx.size());
   }
 };
@@ -578,6 +593,7 @@ template <class VS>
 void draw_elements(VP& vp, const OracleDraw& d) {  // VertexProcessor.cpp:78-120
   vp.verts.clear();
   vp.idx.clear();
+  vp.src.clear();
   int cache_in[16], cache_out[16];  // VertexCache (VertexCache.h:29-63)
   for (int i = 0; i < 16; ++i) cache_in[i] = -1;
   const int per = d.draw_mode == 0 ? 1 : (d.draw_mode == 1 ? 2 : 3);
@@ -596,10 +612,12 @@ void draw_elements(VP& vp, const OracleDraw& d) {  // VertexProcessor.cpp:78-120
       cache_out[slot] = out;
     }
     vp.idx.push_back(out);
+    if (per == 3 && i % 3 == 2) vp.src.push_back((int)(i / 3));
     if ((int)(vp.idx.size() / per) >= kBatchPrims) {
       vp.process();
       vp.verts.clear();
       vp.idx.clear();
+      vp.src.clear();
       for (int k = 0; k < 16; ++k) cache_in[k] = -1;
     }
   }
@@ -667,6 +685,8 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
   if (d->threads > 0) omp_set_num_threads(d->threads);
 #endif
   Counters cnt;
+  cnt.prim_src = d->raster_vertices ? nullptr : d->prim_src;
+  cnt.prim_src_cap = d->prim_src_cap;
   int rc;
   switch (d->ps_id) {
     case SWR_PS_TEX_NEAREST: rc = run_ps<PsTexNearest>(*d, cnt); break;
@@ -683,6 +703,7 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
     st->primitives = cnt.prims;
     st->batches = cnt.batches;
   }
+  if (!rc && cnt.src_overflow) rc = 3;
   return rc;
 }
 

@@ -28,10 +28,12 @@ class SwrDrawItem(ctypes.Structure):
         ("indices", ctypes.c_void_p),
         ("count", ctypes.c_uint64),
         ("uniforms", ctypes.POINTER(SwrUniforms)),
+        ("prim_src", ctypes.c_void_p),
+        ("prim_src_capacity", ctypes.c_uint64),
     ]
 
 
-assert ctypes.sizeof(SwrDrawItem) == 240
+assert ctypes.sizeof(SwrDrawItem) == 256
 
 
 class _PooledTarget:

@@ -7,6 +7,7 @@
 #include <string.h>
 #include <vector>
 #include "../../include/swr_gb300.h"
+#include "swr_context.h"
 #include "swr_core.h"
 #include "swr_ops.h"
 
@@ -80,6 +81,8 @@ struct swr_context {
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
   swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
+  int32_t* prim_src = nullptr;  // swr_set_primitive_source
+  uint64_t prim_src_cap = 0;
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
   // tracing: CUDA events at the stage boundaries of every draw since the last
@@ -196,6 +199,10 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
   D.sc_miny = c->sc_y;
   D.sc_maxx = c->sc_x + c->sc_w;
   D.sc_maxy = c->sc_y + c->sc_h;
+  if (mode == SWR_DRAW_TRIANGLE && c->prim_src) {
+    D.prim_src = c->prim_src;
+    D.prim_src_cap = c->prim_src_cap < 0xffffffffull ? (uint32_t)c->prim_src_cap : 0xffffffffu;
+  }
   D.u = c->u;
 }
 
@@ -443,6 +450,13 @@ int swr_set_uniforms(swr_context* c, const SwrUniforms* u) {
   return SWR_OK;
 }
 
+int swr_set_primitive_source(swr_context* c, int32_t* out, uint64_t capacity) {
+  if (!c || (out && !capacity)) return SWR_EINVAL;
+  c->prim_src = out;
+  c->prim_src_cap = out ? capacity : 0;
+  return SWR_OK;
+}
+
 int swr_set_tile_size(swr_context* c, int tile) {
   if (!c || (tile != 16 && tile != 32)) return SWR_EINVAL;
   c->tile = tile;
@@ -647,6 +661,11 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     d.sc_maxx = it.scissor[0] + it.scissor[2];
     d.sc_maxy = it.scissor[1] + it.scissor[3];
     d.u = u;
+    if (it.prim_src) {
+      if (!it.prim_src_capacity) return SWR_EINVAL;
+      d.prim_src = it.prim_src;
+      d.prim_src_cap = it.prim_src_capacity < 0xffffffffull ? (uint32_t)it.prim_src_capacity : 0xffffffffu;
+    }
     vbase[i] = (uint32_t)V;
     bbase[i] = (uint32_t)B;
     V += nv;
@@ -802,7 +821,8 @@ int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
   cudaMemsetAsync(c->status.p, 0, kStatusWords * 4, s);
   if ((rc = cuda_err(cudaStreamSynchronize(s)))) return rc;
   if (flags & SWR_F_ANY_OVERFLOW) return SWR_EOVERFLOW;
-  if (flags & SWR_F_BAD_INDEX) return SWR_EINDEX;
+  if (flags & (SWR_F_BAD_INDEX | SWR_F_BAD_GRAD_INPUT)) return SWR_EINDEX;
+  if (flags & SWR_F_SRC_OVERFLOW) return SWR_EINVAL;
   return SWR_OK;
 }
 
@@ -842,3 +862,7 @@ const char* swr_status_string(int st) {
 }
 
 }  // extern "C"
+namespace swr {
+uint32_t* context_status(swr_context* c) { return c->status.as<uint32_t>(); }
+void context_add_launches(swr_context* c, uint64_t n) { c->launches += n; }
+}  // namespace swr

@@ -31,6 +31,8 @@ enum SwrStatusFlags {
   SWR_F_PAIR_OVERFLOW = 8,   // bin pair buffer too small
   SWR_F_FRAG_OVERFLOW = 16,  // line/point fragment buffer too small
   SWR_F_CLIP_COMPLEX = 32,   // a clipped polygon exceeded 16 vertices and was dropped
+  SWR_F_SRC_OVERFLOW = 64,   // a caller's primitive-source buffer was too small
+  SWR_F_BAD_GRAD_INPUT = 128,  // backward: a winner or source id beyond the given counts
 };
 #define SWR_F_ANY_OVERFLOW (SWR_F_CLIP_OVERFLOW | SWR_F_PRIM_OVERFLOW | SWR_F_PAIR_OVERFLOW | SWR_F_FRAG_OVERFLOW)
 
@@ -54,7 +56,8 @@ struct SwrDrawDesc {
   float dn, df;                      // VertexProcessor::setDepthRange
   int32_t sc_minx, sc_miny, sc_maxx, sc_maxy;  // Rasterizer::setScissorRect (Rasterizer.h:81-87)
   int32_t direct;     // 1: vertices are RasterizerVertex records already in screen space
-  int32_t _pad;
+  uint32_t prim_src_cap;  // entries of prim_src
+  int32_t* prim_src;  // optional: per emitted primitive (draw-relative id) its source triangle
   SwrUniforms u;
 };
 

@@ -362,10 +362,16 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + half * SWR_HALF;
   const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
-  uint32_t before = 0;
-  for (uint32_t i = threadIdx.x; i < 2 * b; i += blockDim.x) before += g.batch_counts[i].x + g.batch_counts[i].y;
-  uint32_t base;
+  uint32_t before = 0, dbefore = 0;
+  for (uint32_t i = threadIdx.x; i < 2 * b; i += blockDim.x) {
+    const uint32_t c = g.batch_counts[i].x + g.batch_counts[i].y;
+    before += c;
+    if (i < 2 * D.bbase) dbefore += c;
+  }
+  uint32_t base, dbase = 0;
   swr_block_exscan(before, tmp, &base);
+  // the draw's first emitted primitive, for its primitive-source output (uniform per CTA)
+  if (D.prim_src) swr_block_exscan(dbefore, tmp, &dbase);
   const uint2 c0 = g.batch_counts[2 * b], c1 = g.batch_counts[2 * b + 1];
   const uint32_t batch_in = c0.x + c1.x, batch_total = batch_in + c0.y + c1.y;
   // primitive ids seen by the pixel shader are per draw, as with one drawElements call each
@@ -401,12 +407,20 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
     if (threadIdx.x == 0) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
     return;
   }
+  // source triangle (draw-relative) of the primitive emitted at global position `at`
+  auto record_src = [&](uint32_t at, uint32_t src) {
+    if (!D.prim_src) return;
+    const uint32_t k = at - dbase;
+    if (k < D.prim_src_cap) D.prim_src[k] = (int32_t)src;
+    else atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_SRC_OVERFLOW);
+  };
   for (int j = 0; j < 2; ++j) {
     const uint32_t q = threadIdx.x * 2 + j;
     if (!keep[j]) continue;
     if (!(fl[j] & 4)) {
       uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
       if (fl[j] & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
+      record_src(rin, p0 + q);
       g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
     } else {
       // first fan triangle in the input slot, the others after all of the batch's slots
@@ -415,8 +429,13 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
         if (!((e.keep >> k) & 1)) continue;
         uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
         if ((e.swap >> k) & 1) { const uint32_t t = r0; r0 = r2; r2 = t; }
-        if (k == 0) g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
-        else g.tris[rex++] = make_uint4(r0, r1, r2, (uint32_t)d);
+        if (k == 0) {
+          record_src(rin, p0 + q);
+          g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
+        } else {
+          record_src(rex, p0 + q);
+          g.tris[rex++] = make_uint4(r0, r1, r2, (uint32_t)d);
+        }
       }
     }
   }

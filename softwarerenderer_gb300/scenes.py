@@ -563,3 +563,83 @@ def batch_scenes(n: int = 256, seed: int = 4, max_tris: int = 200_000, min_tris:
                          light=np.array([l[0], l[1], l[2], 0.2], np.float32),
                          texture=_mesh_texture(rng, texture_size)))
     return out
+
+
+# ----------------------------------------------------------------------------
+# config: differentiable rendering (forward + backward of PsDiff)
+
+@dataclass
+class DiffProblem:
+    """A mesh seen from several views, rendered with the differentiable shader.
+
+    vertices: (V, 8) float32 records {x, y, z, r, g, b, u, v} (VS.POS_RGB_UV stream 0);
+    indices: (3F,) int32 triangle list; texture: (T, T, 4) float32 RGBA; mvps: one (16,)
+    float32 matrix per view; targets: (views, H, W, 4) float32 images of the L2 loss."""
+    name: str
+    vertices: np.ndarray
+    indices: np.ndarray
+    texture: np.ndarray
+    mvps: List[np.ndarray]
+    targets: np.ndarray
+    width: int
+    height: int
+    cull: CullMode = CullMode.CW
+    raster: RasterMode = RasterMode.Block
+
+    @property
+    def viewport(self):
+        return (0, 0, self.width, self.height)
+
+    @property
+    def n_views(self):
+        return len(self.mvps)
+
+    def scene(self, view: int) -> Scene:
+        """View `view` as an ordinary Scene (for the oracle and single-draw paths)."""
+        return Scene(name=f"{self.name}[{view}]", vs=VS.POS_RGB_UV, ps=PS.DIFF, width=self.width,
+                     height=self.height, cull=self.cull, raster=self.raster, viewport=self.viewport,
+                     scissor=self.viewport, attribs=[(self.vertices, 32)], indices=self.indices,
+                     mvp=self.mvps[view], texture=self.texture)
+
+
+def _smooth_texture(rng, size):
+    """RGBA32F texture from seeded cubic polynomials in (x, y) scaled into [0.15, 0.95] (alpha
+    [0.5, 1]): smooth, so the bilinear interpolant's slope changes little between texels."""
+    t = np.linspace(0.0, 1.0, size)
+    y, x = np.meshgrid(t, t, indexing="ij")
+    out = np.empty((size, size, 4), np.float64)
+    for c in range(4):
+        a = rng.random(10) * 2.0 - 1.0
+        v = (a[0] + a[1] * x + a[2] * y + a[3] * x * x + a[4] * x * y + a[5] * y * y +
+             a[6] * x * x * x + a[7] * x * x * y + a[8] * x * y * y + a[9] * y * y * y)
+        lo, hi = float(v.min()), float(v.max())
+        v = (v - lo) / (hi - lo if hi > lo else 1.0)
+        out[:, :, c] = 0.5 + 0.5 * v if c == 3 else 0.15 + 0.8 * v
+    return out.astype(np.float32)
+
+
+def diff_problem(n_views: int = 16, level: int = 6, size: int = 512, tex_size: int = 1024,
+                 seed: int = 5, raster: RasterMode = RasterMode.Block, clip_views: int = 0,
+                 cull: CullMode = CullMode.CW) -> DiffProblem:
+    """Icosphere at subdivision `level` (level 6: 40,962 v / 81,920 t) with seeded per-vertex
+    RGB in [0.2, 0.8] and planar uv, a `tex_size`^2 RGBA32F texture sampled bilinearly, seen
+    from `n_views` seeded cameras (60 degree perspective, distance in [2.5, 3.5]) at
+    size x size; L2 targets are seeded uniform images.  The first `clip_views` cameras sit
+    at distance 1.11, so the near plane (0.1) cuts the sphere and clipping splits triangles."""
+    rng = np.random.default_rng(seed)
+    p, f = icosphere(level)
+    rgb = rng.random((p.shape[0], 3)) * 0.6 + 0.2
+    uv = np.stack([(p[:, 0] + 1.0) * 0.5, (p[:, 1] + 1.0) * 0.5], 1)
+    verts = np.concatenate([p, rgb, uv], axis=1).astype(np.float32)
+    tex = _smooth_texture(rng, tex_size)
+    mvps = []
+    for k in range(n_views):
+        d = 2.5 + float(rng.random())
+        if k < clip_views:
+            d = 1.11
+        mvps.append(mat_to_f32(_matmul4(perspective(1.0, 0.1, 100.0),
+                                        _matmul4(translate(0.0, 0.0, -d), random_rotation(rng)))))
+    targets = rng.random((n_views, size, size, 4)).astype(np.float32)
+    return DiffProblem(name=f"diff_ico{level}x{n_views}@{size}", vertices=verts,
+                       indices=f.reshape(-1).astype(np.int32), texture=tex, mvps=mvps, targets=targets,
+                       width=size, height=size, raster=raster, cull=cull)
