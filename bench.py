@@ -191,6 +191,7 @@ def main():
     ap.add_argument("--tile", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-rendering section")
     args = ap.parse_args()
     assert args.warmup >= 3, "at least 3 warm-up steps"
 
@@ -299,6 +300,9 @@ def main():
     batched = None
     if not args.no_batch:
         batched = run_batched(torch)
+    diffr = None
+    if not args.no_diff:
+        diffr = run_diff(torch)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -318,7 +322,8 @@ def main():
                 "stage_ms_per_frame": {k: round(v / args.steps, 4) for k, v in stages.items()},
                 "gpu_launches": int(st["launches"]),
                 "roofline": roofline, "frame_roofline": frame_roof,
-                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched}
+                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched,
+                "differentiable": diffr}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -362,6 +367,56 @@ def run_batched(torch, n=256, steps=10):
         res[f"{mode}_views_per_s"] = round(n / (ms / 1e3), 1)
     res["speedup_vs_loop"] = round(res["batch_views_per_s"] / res["loop_views_per_s"], 3)
     res["batch_mtris_per_s"] = round(res["triangles_per_step"] / (res["batch_ms_per_step"] / 1e3) / 1e6, 1)
+    return res
+
+
+def run_diff(torch, steps=20, warmup=3):
+    """Differentiable rendering: 16 views of the level-6 icosphere (40,962 vertices, 81,920
+    triangles) at 512x512, per-vertex RGB and uv sampling a 1024x1024 RGBA32F texture
+    bilinearly, L2 loss against seeded targets.  `fwd` = clearing the 16 targets + one
+    swr_draw_batch (CUDA graph replay); `fwd_bwd` = fwd + zeroing the gradient buffers +
+    swr_backward with the fused L2 loss (dL/d vertex records, dL/d texels, loss).  L2 is
+    flushed (256 MiB write) before every step; every step is timed with CUDA events."""
+    from softwarerenderer_gb300 import scenes
+    from softwarerenderer_gb300.diff import DiffRenderer
+    P = scenes.diff_problem()
+    dr = DiffRenderer(P.indices, P.vertices.shape[0], P.texture.shape[1], P.texture.shape[0], P.mvps,
+                      P.width, P.height, cull=P.cull, raster=P.raster)
+    v = torch.from_numpy(P.vertices).cuda()
+    t = torch.from_numpy(P.texture).cuda()
+    tg = torch.from_numpy(P.targets).cuda()
+    gv, gt = torch.zeros_like(v), torch.zeros_like(t)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    for _ in range(warmup):
+        dr.forward(v, t)
+        gv.zero_()
+        gt.zero_()
+        dr.backward(v, t, target=tg, grad_vertices=gv, grad_texture=gt)
+    res = {"workload": "16 views of icosphere-6 (81,920 triangles) at 512x512, 1024x1024 RGBA32F texture, L2 loss",
+           "views": P.n_views, "triangles_per_view": len(P.indices) // 3}
+    for mode in ("fwd", "fwd_bwd"):
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+        torch.cuda.synchronize()
+        for k in range(steps):
+            flush.fill_(k)
+            ev[k][0].record()
+            dr.forward(v, t, sync=False)
+            ev[k][1].record()
+            if mode == "fwd_bwd":
+                gv.zero_()
+                gt.zero_()
+                dr.backward(v, t, target=tg, grad_vertices=gv, grad_texture=gt, sync=False)
+            ev[k][2].record()
+        torch.cuda.synchronize()
+        rc, st = dr.ctx.finish()
+        assert rc == 0, rc
+        res[f"{mode}_ms"] = round(sum(e[0].elapsed_time(e[2]) for e in ev) / steps, 4)
+        if mode == "fwd_bwd":
+            res["bwd_ms"] = round(sum(e[1].elapsed_time(e[2]) for e in ev) / steps, 4)
+    res["fwd_views_per_s"] = round(P.n_views / (res["fwd_ms"] / 1e3), 1)
+    res["fwd_bwd_views_per_s"] = round(P.n_views / (res["fwd_bwd_ms"] / 1e3), 1)
+    res["fwd_bwd_over_fwd"] = round(res["fwd_bwd_ms"] / res["fwd_ms"], 3)
+    res["covered_pixels"] = int((dr.winner >= 0).sum())
     return res
 
 

@@ -190,6 +190,18 @@ typedef struct swr_backward_args {
 int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad_view* views, int nviews,
                  void* stream);
 
+/* Mip-mapped texturing (the reference's example texture, src/examples/Texture.h, used by
+ * its Box example).  SWR_PS_TEX_MIP samples SwrUniforms.tex as a mip chain: level 0 of
+ * tex_w x tex_h 0x00RRGGBB texels followed by every smaller level down to 1 x 1, each
+ * max(1, w/2) x max(1, h/2) of the one before, anisotropically (up to
+ * SwrUniforms.max_aniso taps, 0 = 8) with the footprint from
+ * PixelData::computePerspectiveDerivatives (PixelData.h:128-145).
+ * swr_mip_chain_size gives the level count and the total texels of the chain;
+ * swr_build_mip_chain fills it from a level-0 image (Texture::generateMipmaps,
+ * Texture.h:220-293; 2 x 2 box filter).  Both buffers are device memory. */
+int swr_mip_chain_size(int width, int height, int* levels, uint64_t* texels);
+int swr_build_mip_chain(const uint32_t* base, int width, int height, uint32_t* chain, void* stream);
+
 /* Allocation-free triangle-list draw.  No counterpart in the reference (whose CPU
  * rasterizer needs no device scratch).  It is swr_draw_list(SWR_DRAW_TRIANGLE, ...) for
  * callers that must not allocate device memory -- an application whose device memory is

@@ -89,6 +89,9 @@ def load(which="port"):
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
             lib.oracle_diff_fd.restype = ctypes.c_int
+        if hasattr(lib, "oracle_log2"):
+            lib.oracle_log2.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+            lib.oracle_log2.restype = None
         if hasattr(lib, "oracle_fold_selftest"):
             lib.oracle_fold_selftest.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
             lib.oracle_fold_selftest.restype = ctypes.c_uint64
@@ -108,6 +111,13 @@ class Oracle:
     def fold(self, v, a, k):
         return self.lib.oracle_fold(v, a, k)
 
+    def log2(self, x):
+        """swr_log2 (the texture sampler's level-of-detail logarithm) of a float32 array."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty_like(x)
+        self.lib.oracle_log2(x.ctypes.data, out.ctypes.data, x.size)
+        return out
+
     def draw(self, scene, target, threads=0, prim_src=None):
         """Render `scene` into `target` (numpy buffers, modified in place); returns stats.
         `prim_src` (int32 array, port only) receives the source triangle of every primitive."""
@@ -116,11 +126,12 @@ class Oracle:
         if tex is not None:
             tex = np.ascontiguousarray(tex)
             keep.append(tex)
+        tw, th = scene.texture_wh()
         u = make_uniforms(scene.mvp, scene.light, scene.checker, scene.width, scene.height,
-                          tex_ptr=_ptr(tex), tex_w=tex.shape[1] if tex is not None else 0,
-                          tex_h=tex.shape[0] if tex is not None else 0,
+                          tex_ptr=_ptr(tex), tex_w=tw, tex_h=th,
                           color=_ptr(target.color), depth=_ptr(target.depth),
-                          frag_count=_ptr(target.frag_count), winner=_ptr(target.winner))
+                          frag_count=_ptr(target.frag_count), winner=_ptr(target.winner),
+                          max_aniso=scene.max_aniso)
         d = OracleDraw()
         d.vs_id, d.ps_id = int(scene.vs), int(scene.ps)
         d.draw_mode, d.cull_mode, d.raster_mode = int(scene.draw_mode), int(scene.cull), int(scene.raster)

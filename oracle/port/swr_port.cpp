@@ -80,9 +80,11 @@ struct Pix {
   int x, y;
   float z, w, invw;
   float avar[kMaxVars], pvar[kMaxVars], pvarTemp[kMaxVars];
+  const TriEq* eq = nullptr;  // PixelData::equations (set by init; null for points and lines)
   enum { NA = PS::AVarCount, NP = PS::PVarCount, IZ = PS::InterpolateZ,
          IW = PS::InterpolateW || PS::PVarCount > 0 };
   void init(const TriEq& e, float fx, float fy) {  // PixelData.h:61-79
+    eq = &e;
     if (IZ) z = e.z.eval(fx, fy);
     if (IW) { invw = e.invw.eval(fx, fy); w = 1.0f / invw; }
     for (int i = 0; i < NA; ++i) avar[i] = e.avar[i].eval(fx, fy);
@@ -101,6 +103,19 @@ struct Pix {
     for (int i = 0; i < NP; ++i) { pvarTemp[i] = pvarTemp[i] + e.pvar[i].b; pvar[i] = pvarTemp[i] * w; }
   }
 };
+
+// PixelData::computePerspectiveDerivatives (PixelData.h:128-145) for the shared shaders
+// (found by argument-dependent lookup).
+template <class PS>
+void swr_persp_deriv(const Pix<PS>& p, int i, float& ddx, float& ddy) {
+  if (!p.eq) {
+    ddx = ddy = 0.0f;
+    return;
+  }
+  const float pv[3] = {p.eq->pvar[i].a, p.eq->pvar[i].b, p.eq->pvar[i].c};
+  const float iw[3] = {p.eq->invw.a, p.eq->invw.b, p.eq->invw.c};
+  swr_persp_deriv_eq(pv, iw, p.x, p.y, ddx, ddy);
+}
 
 struct Counters {
   uint64_t frags = 0, outside = 0, prims = 0, batches = 0;
@@ -695,6 +710,8 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
     case SWR_PS_VCOLOR_AFFINE: rc = run_ps<PsVColorAffine>(*d, cnt); break;
     case SWR_PS_LAMBERT_TEX: rc = run_ps<PsLambertTex>(*d, cnt); break;
     case SWR_PS_DIFF: rc = run_ps<PsDiff>(*d, cnt); break;
+    case SWR_PS_TEX_MIP: rc = d->draw_mode == 2 ? run_ps<PsTexMip>(*d, cnt) : 1; break;
+    case SWR_PS_PERSP_DERIV: rc = d->draw_mode == 2 ? run_ps<PsPerspDeriv>(*d, cnt) : 1; break;
     default: rc = 2;
   }
   if (st) {
@@ -708,6 +725,11 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
 }
 
 extern "C" float oracle_fold(float v, float a, int k) { return swr_fold(v, a, k); }
+
+// swr_log2 and the mip-mapped sampler exposed for the tests of the texture subsystem.
+extern "C" void oracle_log2(const float* x, float* out, uint64_t n) {
+  for (uint64_t i = 0; i < n; ++i) out[i] = swr_log2(x[i]);
+}
 
 // Randomized check of swr_fold against plain serial stepping: returns the number of
 // (v, a, k) cases where they differ (NaN results compare equal).  Cases mix arbitrary bit

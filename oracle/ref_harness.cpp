@@ -9,6 +9,14 @@
 #include "Renderer.h"  // reference umbrella header (src/renderer/Renderer.h)
 #include "oracle_abi.h"
 
+namespace swr {
+// The shared shaders ask for derivatives through swr_persp_deriv (argument-dependent
+// lookup): here it is the reference's own PixelData::computePerspectiveDerivatives.
+inline void swr_persp_deriv(const PixelData& p, int i, float& ddx, float& ddy) {
+  p.computePerspectiveDerivatives(*p.equations, i, ddx, ddy);
+}
+}  // namespace swr
+
 namespace {
 
 const SwrUniforms* g_u = nullptr;  // the reference keeps shader parameters in statics
@@ -112,6 +120,9 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
     case SWR_PS_VCOLOR_AFFINE: set_ps<PsVColorAffine>(r); break;
     case SWR_PS_LAMBERT_TEX: set_ps<PsLambertTex>(r); break;
     case SWR_PS_DIFF: set_ps<PsDiff>(r); break;
+    // equations are set only for triangles (points and lines would dereference null)
+    case SWR_PS_TEX_MIP: if (d->draw_mode != 2) return 1; set_ps<PsTexMip>(r); break;
+    case SWR_PS_PERSP_DERIV: if (d->draw_mode != 2) return 1; set_ps<PsPerspDeriv>(r); break;
     default: return 2;
   }
   NumberingRasterizer nr(&r);

@@ -48,6 +48,8 @@ class PS(enum.IntEnum):
     VCOLOR_AFFINE = 4
     LAMBERT_TEX = 5
     DIFF = 6
+    TEX_MIP = 7
+    PERSP_DERIV = 8
 
 
 # (AttribCount, AVarCount, PVarCount) of each vertex shader, and
@@ -56,7 +58,10 @@ VS_INFO = {VS.POS_UV: (1, 0, 2), VS.POS_NRM_UV: (2, 3, 2), VS.POS_RGB: (1, 0, 3)
            VS.POS_RGB_AFFINE: (1, 3, 0), VS.POS_RGB_UV: (1, 0, 5)}
 PS_INFO = {PS.TEX_NEAREST: (0, 2, 1, 1, 1, 0), PS.LAMBERT: (3, 2, 1, 1, 1, 0),
            PS.VCOLOR: (0, 3, 1, 1, 1, 0), PS.VCOLOR_AFFINE: (3, 0, 0, 0, 0, 0),
-           PS.LAMBERT_TEX: (3, 2, 1, 1, 1, 0), PS.DIFF: (0, 5, 1, 1, 1, 1)}
+           PS.LAMBERT_TEX: (3, 2, 1, 1, 1, 0), PS.DIFF: (0, 5, 1, 1, 1, 1),
+           PS.TEX_MIP: (0, 2, 0, 1, 0, 0), PS.PERSP_DERIV: (0, 2, 1, 1, 1, 1)}
+# Pixel shaders that read the triangle equations (triangles only).
+PS_NEEDS_EQUATIONS = {PS.TEX_MIP, PS.PERSP_DERIV}
 
 # Floats per RasterizerVertex (IRasterizer.h:42-53): x, y, z, w, avar[16], pvar[16].
 RASTER_VERTEX_FLOATS = 36
@@ -76,7 +81,7 @@ class SwrUniforms(ctypes.Structure):
         ("width", ctypes.c_int32),
         ("height", ctypes.c_int32),
         ("checker", ctypes.c_int32),
-        ("_pad", ctypes.c_int32),
+        ("max_aniso", ctypes.c_int32),
     ]
 
 
@@ -84,7 +89,7 @@ assert ctypes.sizeof(SwrUniforms) == 144
 
 
 def make_uniforms(mvp, light, checker, width, height, tex_ptr=0, tex_w=0, tex_h=0,
-                  color=0, depth=0, frag_count=0, winner=0):
+                  color=0, depth=0, frag_count=0, winner=0, max_aniso=0):
     u = SwrUniforms()
     m = np.asarray(mvp, dtype=np.float32).reshape(16)
     for i in range(16):
@@ -100,4 +105,5 @@ def make_uniforms(mvp, light, checker, width, height, tex_ptr=0, tex_w=0, tex_h=
     u.winner = winner or None
     u.width, u.height = int(width), int(height)
     u.checker = int(checker)
+    u.max_aniso = int(max_aniso)
     return u

@@ -177,16 +177,10 @@ __device__ __forceinline__ void pixel_backward(const BwdView& V, const BwdArgs& 
   }
 }
 
-__global__ void __launch_bounds__(256) k_backward(const __grid_constant__ BwdViews views, const BwdArgs a) {
-  __shared__ BwdView V;
+__global__ void __launch_bounds__(256, 4) k_backward(const __grid_constant__ BwdViews views, const BwdArgs a) {
   __shared__ float red[8];
-  if ((int)blockIdx.x >= views.v[blockIdx.y].tiles) return;  // uniform per CTA
-  {
-    const uint32_t* src = (const uint32_t*)&views.v[blockIdx.y];
-    uint32_t* dst = (uint32_t*)&V;
-    for (int i = threadIdx.x; i < (int)(sizeof(BwdView) / 4); i += blockDim.x) dst[i] = src[i];
-  }
-  __syncthreads();
+  const BwdView& V = views.v[blockIdx.y];  // kernel parameter space: uniform constant loads
+  if ((int)blockIdx.x >= V.tiles) return;  // uniform per CTA
   const int tx = (int)blockIdx.x % V.tiles_x, ty = (int)blockIdx.x / V.tiles_x;
   const int x = tx * kTile + (int)(threadIdx.x % kTile), y = ty * kTile + (int)(threadIdx.x / kTile);
   float lsum = 0.0f;

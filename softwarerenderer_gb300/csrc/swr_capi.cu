@@ -469,6 +469,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   const PsOps* ps = ps_ops(c->ps_id);
   if (!vs || !ps) return SWR_EINVAL;
   if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
+  if (ps->needs_eq && mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // PixelData::equations is null
   const uint64_t per = mode == SWR_DRAW_POINT ? 1 : (mode == SWR_DRAW_LINE ? 2 : 3);
   if (count % per || count / per >= 0x7fffffffull || (count && !indices)) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
@@ -541,6 +542,7 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   const PsOps* ps = ps_ops(c->ps_id);
   if (!ps) return SWR_EINVAL;
   if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
+  if (ps->needs_eq && mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // PixelData::equations is null
   const int per = mode == SWR_DRAW_POINT ? 1 : (mode == SWR_DRAW_LINE ? 2 : 3);
   if (count % per || count / per >= 0x7fffffffull || nverts >= 0x7fffffffull) return SWR_EINVAL;
   if ((count && !indices) || (nverts && !vertices)) return SWR_EINVAL;

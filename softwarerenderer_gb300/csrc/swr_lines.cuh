@@ -299,6 +299,7 @@ __global__ void __launch_bounds__(256) k_lp_shade(LpShadeArgs g) {
       GpuPixel<PS> pd;
       pd.x = x;
       pd.y = y;
+      pd.eq = nullptr;  // points and lines carry no triangle equations
       if (PS::InterpolateZ) pd.z = lp_value<PS>(rec, 2, j);
       if (PS::InterpolateW) {
         pd.w = lp_value<PS>(rec, 3, j);

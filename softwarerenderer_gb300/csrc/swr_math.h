@@ -15,6 +15,7 @@
 // contracted into FMA); the host relies on -ffp-contract=off and SSE/NEON scalar
 // float arithmetic.
 #pragma once
+#include <math.h>
 #include <stdint.h>
 #ifndef __CUDACC__
 #include <string.h>
@@ -183,4 +184,82 @@ SWR_HD float swr_fold(float v, float a, int k) {
     k -= m;
   }
   return v;
+}
+
+// ---------------------------------------------------------------------------
+// Helpers of the texture sampler (exact on both sides: fmod, floor and ceil are exact
+// operations; log2 is computed here from binary64 +, -, *, / only).
+
+SWR_HD float swr_fmodf(float a, float b) { return fmodf(a, b); }
+SWR_HD float swr_floorf(float a) { return floorf(a); }
+SWR_HD float swr_ceilf(float a) { return ceilf(a); }
+SWR_HD bool swr_isnan(float a) { return a != a; }
+
+SWR_HD double swr_dadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+SWR_HD double swr_dsub(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+SWR_HD double swr_dmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+SWR_HD double swr_ddiv(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// log2(x) rounded to binary32, identical on every IEEE-754 machine.  x = m * 2^e with m in
+// [sqrt(1/2), sqrt(2)); ln m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...), s = (m - 1) / (m + 1),
+// |s| < 0.1716 (the series ln((1 + s) / (1 - s)), Abramowitz & Stegun 4.1.28), summed in
+// binary64 to s^23 (truncation below 1e-19 relative), scaled by 1/ln 2 and rounded once.
+// Special values: log2(+0) = -inf, log2(+inf) = +inf, negative or NaN input -> NaN.
+SWR_HD float swr_log2(float x) {
+  if (!(x > 0.0f)) return x == 0.0f ? -INFINITY : NAN;
+  uint32_t b = swr_f2u(x);
+  if (b >= 0x7f800000u) return x;  // +inf
+  int e = 0;
+  if (b < 0x00800000u) {  // subnormal: scale by 2^32 into the normal range
+    b = swr_f2u(swr_mul(x, 4294967296.0f));
+    e = -32;
+  }
+  e += (int)(b >> 23) - 127;
+  float m = swr_u2f((b & 0x007fffffu) | 0x3f800000u);  // [1, 2)
+  if (m > 1.41421353816986083984375f) {  // sqrt(2) rounded down to binary32
+    m = swr_mul(m, 0.5f);
+    e += 1;
+  }
+  const double md = (double)m;
+  const double s = swr_ddiv(swr_dsub(md, 1.0), swr_dadd(md, 1.0));
+  const double s2 = swr_dmul(s, s);
+  double poly = 1.0 / 23.0;
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 21.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 19.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 17.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 15.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 13.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 11.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 9.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 7.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 5.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0 / 3.0);
+  poly = swr_dadd(swr_dmul(poly, s2), 1.0);
+  const double ln_m = swr_dmul(2.0, swr_dmul(s, poly));
+  const double inv_ln2 = 1.4426950408889634;  // 1 / ln 2 rounded to binary64
+  return (float)swr_dadd((double)e, swr_dmul(ln_m, inv_ln2));
 }

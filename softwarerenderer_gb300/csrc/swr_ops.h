@@ -34,6 +34,7 @@ struct PsOps {
   void (*lp_setup)(const SetupArgs& a, cudaStream_t s);
   void (*lp_frags)(const LpFragArgs& a, cudaStream_t s);
   void (*lp_shade)(const LpShadeArgs& a, cudaStream_t s);
+  int needs_eq;  // shade() reads the triangle equations: triangles only
 };
 
 const VsOps* vs_ops(int id);

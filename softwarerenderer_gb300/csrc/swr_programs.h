@@ -43,7 +43,7 @@ struct SwrUniforms {
   int32_t* winner;        // optional: per-pixel primitive id of the last colour write
   int32_t width, height;  // render target size in pixels; row pitch == width
   int32_t checker;        // checker squares per unit of uv for procedural albedo
-  int32_t _pad;
+  int32_t max_aniso;      // mip-mapped sampler: anisotropic sample limit (0 = 8, the default)
 };
 
 // Vertex attribute pointers as handed to VS::processVertex (VertexConfig.h:34-40).
@@ -427,8 +427,238 @@ struct PsDiff {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Mip-mapped texture sampling: a restatement of the reference's example texture
+// (src/examples/Texture.h) for a mip chain held in device memory.  Texels are packed
+// 0x00RRGGBB (the SDL surface format of Texture.h:225-231: R in bits 16-23); the chain is
+// level 0 (tex_w x tex_h) followed by every smaller level down to 1 x 1, each
+// max(1, w / 2) x max(1, h / 2) of the one before (Texture.h:246-290).
+
+// Number of levels of the chain of a w x h texture.
+SWR_HD int swr_mip_levels(int w, int h) {
+  int n = 1;
+  while (w > 1 || h > 1) {
+    w = swr_maxi(1, w / 2);
+    h = swr_maxi(1, h / 2);
+    ++n;
+  }
+  return n;
+}
+
+struct SwrMip {
+  const uint32_t* p;
+  int w, h;
+};
+
+SWR_HD SwrMip swr_mip_level(const SwrUniforms& u, int level) {
+  SwrMip m;
+  m.p = (const uint32_t*)u.tex;
+  m.w = u.tex_w;
+  m.h = u.tex_h;
+  for (int l = 0; l < level; ++l) {
+    m.p += (size_t)m.w * (size_t)m.h;
+    m.w = swr_maxi(1, m.w / 2);
+    m.h = swr_maxi(1, m.h / 2);
+  }
+  return m;
+}
+
+SWR_HD uint32_t swr_rgb_channel(uint32_t c, int sh) { return (c >> sh) & 0xffu; }
+
+// Texture::lerpColors (Texture.h:191-196).  The reference converts the possibly negative
+// float (c2 - c1) * t straight to Uint8, which C++ leaves undefined; this takes the
+// x86-64 result (truncate toward zero, keep the low 8 bits), i.e. c1 + trunc(d * t)
+// wrapped to 8 bits -- the intended linear interpolation.
+SWR_HD uint32_t swr_rgb_lerp(uint32_t c1, uint32_t c2, float t) {
+  uint32_t out = 0;
+  for (int sh = 16; sh >= 0; sh -= 8) {
+    const int a = (int)swr_rgb_channel(c1, sh), b = (int)swr_rgb_channel(c2, sh);
+    const int d = swr_trunc_int(swr_mul((float)(b - a), t));
+    out |= ((uint32_t)(a + d) & 0xffu) << sh;
+  }
+  return out;
+}
+
+// Texture::bilinearLerpColors (Texture.h:198-218): per channel
+// ((c00*(1-fx))*(1-fy) + (c10*fx)*(1-fy)) + (c01*(1-fx))*fy + (c11*fx)*fy, truncated.
+SWR_HD uint32_t swr_rgb_bilerp(uint32_t c00, uint32_t c10, uint32_t c01, uint32_t c11, float fx, float fy) {
+  const float gx = swr_sub(1.0f, fx), gy = swr_sub(1.0f, fy);
+  uint32_t out = 0;
+  for (int sh = 16; sh >= 0; sh -= 8) {
+    float v = swr_mul(swr_mul((float)swr_rgb_channel(c00, sh), gx), gy);
+    v = swr_add(v, swr_mul(swr_mul((float)swr_rgb_channel(c10, sh), fx), gy));
+    v = swr_add(v, swr_mul(swr_mul((float)swr_rgb_channel(c01, sh), gx), fy));
+    v = swr_add(v, swr_mul(swr_mul((float)swr_rgb_channel(c11, sh), fx), fy));
+    out |= ((uint32_t)swr_trunc_int(v) & 0xffu) << sh;
+  }
+  return out;
+}
+
+// Texture::sampleBilinear (Texture.h:146-181) on one level; u, v in [0, 1].
+SWR_HD uint32_t swr_sample_bilinear(const SwrMip& m, float u, float v) {
+  const float px = swr_mul(u, (float)(m.w - 1));
+  const float py = swr_mul(v, (float)(m.h - 1));
+  const int x0 = swr_maxi(0, swr_trunc_int(swr_floorf(px)));
+  const int y0 = swr_maxi(0, swr_trunc_int(swr_floorf(py)));
+  const int x1 = swr_mini(m.w - 1, x0 + 1);
+  const int y1 = swr_mini(m.h - 1, y0 + 1);
+  const float fx = swr_sub(px, (float)x0);
+  const float fy = swr_sub(py, (float)y0);
+  const size_t w = (size_t)m.w;
+  return swr_rgb_bilerp(m.p[(size_t)y0 * w + x0], m.p[(size_t)y0 * w + x1], m.p[(size_t)y1 * w + x0],
+                        m.p[(size_t)y1 * w + x1], fx, fy);
+}
+
+SWR_HD float swr_clampf(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }  // std::clamp
+
+// Texture::sampleTrilinear (Texture.h:122-144).  A NaN footprint (the reference then
+// converts NaN to int, which is undefined) samples level 0.
+SWR_HD uint32_t swr_sample_trilinear(const SwrUniforms& t, float u, float v, float rho) {
+  const int levels = swr_mip_levels(t.tex_w, t.tex_h);
+  float lod = swr_log2(swr_maxf(rho, 1e-6f));
+  if (swr_isnan(lod)) lod = 0.0f;
+  lod = swr_clampf(lod, 0.0f, (float)(levels - 1));
+  const int base = swr_trunc_int(swr_floorf(lod));
+  const int next = swr_mini(base + 1, levels - 1);
+  const float frac = swr_clampf(swr_sub(lod, (float)base), 0.0f, 1.0f);
+  const uint32_t cb = swr_sample_bilinear(swr_mip_level(t, base), u, v);
+  if (base == next) return cb;
+  return swr_rgb_lerp(cb, swr_sample_bilinear(swr_mip_level(t, next), u, v), frac);
+}
+
+// u mod 1 into [0, 1) as Texture::sample wraps it (Texture.h:42-45); NaN (undefined
+// downstream in the reference) wraps to 0.
+SWR_HD float swr_wrap01(float u) {
+  u = swr_fmodf(u, 1.0f);
+  if (u < 0.0f) u = swr_add(u, 1.0f);
+  return swr_isnan(u) ? 0.0f : u;
+}
+
+// Texture::sample (Texture.h:35-119): anisotropic filtering along the major axis of the
+// pixel footprint, up to max_aniso trilinear taps.  Derivatives come from
+// PixelData::computePerspectiveDerivatives.
+SWR_HD uint32_t swr_tex_sample(const SwrUniforms& t, float u, float v, float dudx, float dvdx, float dudy,
+                               float dvdy) {
+  u = swr_wrap01(u);
+  v = swr_wrap01(v);
+  const float fw = (float)t.tex_w, fh = (float)t.tex_h;
+  const float dudx_s = swr_mul(dudx, fw), dvdx_s = swr_mul(dvdx, fh);
+  const float dudy_s = swr_mul(dudy, fw), dvdy_s = swr_mul(dvdy, fh);
+  float dx_len = swr_sqrt(swr_add(swr_mul(dudx_s, dudx_s), swr_mul(dvdx_s, dvdx_s)));
+  float dy_len = swr_sqrt(swr_add(swr_mul(dudy_s, dudy_s), swr_mul(dvdy_s, dvdy_s)));
+  dx_len = swr_maxf(dx_len, 1e-6f);
+  dy_len = swr_maxf(dy_len, 1e-6f);
+  const float major = swr_maxf(dx_len, dy_len);
+  const float minor = swr_minf(dx_len, dy_len);
+  const int aniso = t.max_aniso > 0 ? swr_mini(t.max_aniso, 16) : 8;  // Texture.h:13-17
+  const float ratio = swr_minf(swr_div(major, minor), (float)aniso);
+  const int n = swr_isnan(ratio) ? 1 : swr_maxi(1, swr_trunc_int(swr_ceilf(ratio)));
+  if (n <= 1) return swr_sample_trilinear(t, u, v, major);
+  float mdu, mdv;
+  if (dx_len > dy_len) {
+    mdu = swr_div(dudx, dx_len);
+    mdv = swr_div(dvdx, dx_len);
+  } else {
+    mdu = swr_div(dudy, dy_len);
+    mdv = swr_div(dvdy, dy_len);
+  }
+  float r = 0.0f, g = 0.0f, b = 0.0f;
+  const float step = swr_div(1.0f, (float)n);
+  for (int i = 0; i < n; ++i) {
+    const float k = swr_sub(swr_mul(swr_add((float)i, 0.5f), step), 0.5f);
+    const float su = swr_wrap01(swr_add(u, swr_mul(swr_mul(mdu, major), k)));
+    const float sv = swr_wrap01(swr_add(v, swr_mul(swr_mul(mdv, major), k)));
+    const uint32_t c = swr_sample_trilinear(t, su, sv, minor);
+    r = swr_add(r, (float)swr_rgb_channel(c, 16));
+    g = swr_add(g, (float)swr_rgb_channel(c, 8));
+    b = swr_add(b, (float)swr_rgb_channel(c, 0));
+  }
+  const float fn = (float)n;
+  r = swr_minf(255.0f, swr_div(r, fn));
+  g = swr_minf(255.0f, swr_div(g, fn));
+  b = swr_minf(255.0f, swr_div(b, fn));
+  return ((uint32_t)swr_trunc_int(r) << 16) | ((uint32_t)swr_trunc_int(g) << 8) | (uint32_t)swr_trunc_int(b);
+}
+
+// Mip-mapped textured shader of the reference's Box example (Box.cpp:40-66): no depth
+// test, every fragment overwrites the pixel with the anisotropic sample at (u, v), its
+// footprint from the perspective-correct derivatives of u and v.  PVar = uv.
+struct PsTexMip {
+  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 0, InterpolateW = 1, HasDepth = 0, NeedsEquations = 1 };
+  typedef SwrStateRGBA8 State;
+  SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<false>(s, x, y, u); }
+  SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, false); }
+  SWR_HD static bool earlyReject(float, State&) { return false; }
+  typedef uint32_t Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms& u) {
+    float dudx, dudy, dvdx, dvdy;
+    swr_persp_deriv(p, 0, dudx, dudy);
+    swr_persp_deriv(p, 1, dvdx, dvdy);
+    return swr_tex_sample(u, p.pvar[0], p.pvar[1], dudx, dvdx, dudy, dvdy);
+  }
+  SWR_HD static void apply(State& s, float, Color c, int prim) {
+    s.frags++;
+    s.color = c;
+    s.winner = prim;
+    s.writes++;
+  }
+  template <class PD>
+  SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
+    apply(s, 0.0f, shade(p, u), prim);
+  }
+};
+
+// Writes the perspective-correct derivatives of pvar 0 and 1 (PixelData.h:128-145) as
+// RGBA32F (du/dx, du/dy, dv/dx, dv/dy), depth-tested: the derivative path itself.
+struct PsPerspDeriv {
+  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, NeedsEquations = 1 };
+  typedef SwrStateRGBA32F State;
+  SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { PsDiff::load(s, x, y, u); }
+  SWR_HD static bool earlyReject(float z, State& s) { return swr_depth_reject(z, s); }
+  SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { PsDiff::store(s, x, y, u); }
+  typedef PsDiff::Color Color;
+  template <class PD>
+  SWR_HD static Color shade(const PD& p, const SwrUniforms&) {
+    Color o;
+    swr_persp_deriv(p, 0, o.c[0], o.c[1]);
+    swr_persp_deriv(p, 1, o.c[2], o.c[3]);
+    return o;
+  }
+  SWR_HD static void apply(State& s, float z, const Color& c, int prim) { PsDiff::apply(s, z, c, prim); }
+  template <class PD>
+  SWR_HD static void drawPixel(const PD& p, int prim, State& s, const SwrUniforms& u) {
+    s.frags++;
+    if (p.z < s.depth) PsDiff::write(s, p.z, shade(p, u), prim);
+  }
+};
+
+// PixelData::computePerspectiveDerivatives (PixelData.h:128-145) from the triangle's
+// parameter equations (a, b, c per equation, evaluated ((a x) + (b y)) + c at the pixel
+// centre): d(var/invw) by the quotient rule, in the reference's operation order.
+SWR_HD void swr_persp_deriv_eq(const float* pv, const float* iw, int x, int y, float& ddx, float& ddy) {
+  const float fx = swr_add((float)x, 0.5f), fy = swr_add((float)y, 0.5f);
+  const float var = swr_eval(pv[0], pv[1], pv[2], fx, fy);
+  const float inv = swr_eval(iw[0], iw[1], iw[2], fx, fy);
+  const float den = swr_mul(inv, inv);
+  ddx = swr_div(swr_sub(swr_mul(inv, pv[0]), swr_mul(var, iw[0])), den);
+  ddy = swr_div(swr_sub(swr_mul(inv, pv[1]), swr_mul(var, iw[1])), den);
+}
+
 // Program registry ids (stable C-ABI values).
 enum SwrVsId { SWR_VS_POS_UV = 1, SWR_VS_POS_NRM_UV = 2, SWR_VS_POS_RGB = 3,
                SWR_VS_POS_RGB_AFFINE = 4, SWR_VS_POS_RGB_UV = 5 };
 enum SwrPsId { SWR_PS_TEX_NEAREST = 1, SWR_PS_LAMBERT = 2, SWR_PS_VCOLOR = 3,
-               SWR_PS_VCOLOR_AFFINE = 4, SWR_PS_LAMBERT_TEX = 5, SWR_PS_DIFF = 6 };
+               SWR_PS_VCOLOR_AFFINE = 4, SWR_PS_LAMBERT_TEX = 5, SWR_PS_DIFF = 6,
+               SWR_PS_TEX_MIP = 7, SWR_PS_PERSP_DERIV = 8 };
+
+// Pixel shaders whose shade() reads the triangle's equations (PixelData::equations) --
+// set only for triangles; the reference dereferences a null pointer for points and lines.
+template <class PS, class = void>
+struct SwrNeedsEquations {
+  enum { value = 0 };
+};
+template <class PS>
+struct SwrNeedsEquations<PS, decltype((void)PS::NeedsEquations)> {
+  enum { value = PS::NeedsEquations };
+};

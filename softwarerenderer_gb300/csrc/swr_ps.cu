@@ -76,6 +76,7 @@ PsOps make() {
   o.lp_setup = &run_lp_setup<PS>;
   o.lp_frags = &run_lp_frags<PS>;
   o.lp_shade = &run_lp_shade<PS>;
+  o.needs_eq = SwrNeedsEquations<PS>::value;
   return o;
 }
 
@@ -85,6 +86,8 @@ const PsOps kVColor = make<PsVColor>();
 const PsOps kVColorAffine = make<PsVColorAffine>();
 const PsOps kLambertTex = make<PsLambertTex>();
 const PsOps kDiff = make<PsDiff>();
+const PsOps kTexMip = make<PsTexMip>();
+const PsOps kPerspDeriv = make<PsPerspDeriv>();
 
 }  // namespace
 
@@ -96,6 +99,8 @@ const PsOps* ps_ops(int id) {
     case SWR_PS_VCOLOR_AFFINE: return &kVColorAffine;
     case SWR_PS_LAMBERT_TEX: return &kLambertTex;
     case SWR_PS_DIFF: return &kDiff;
+    case SWR_PS_TEX_MIP: return &kTexMip;
+    case SWR_PS_PERSP_DERIV: return &kPerspDeriv;
     default: return nullptr;
   }
 }

@@ -883,7 +883,20 @@ struct GpuPixel {  // PixelData (PixelData.h:35-146) as seen by drawPixel
   float z, w, invw;
   float avar[PS::AVarCount > 0 ? PS::AVarCount : 1];
   float pvar[PS::PVarCount > 0 ? PS::PVarCount : 1];
+  const float* eq;  // the triangle's parameter equations (PixelData::equations); null for points and lines
 };
+
+// PixelData::computePerspectiveDerivatives(*equations, i, ddx, ddy) for the pixel shaders
+// (found by argument-dependent lookup from swr_programs.h).
+template <class PS>
+__device__ __forceinline__ void swr_persp_deriv(const GpuPixel<PS>& p, int i, float& ddx, float& ddy) {
+  if (!p.eq) {
+    ddx = ddy = 0.0f;
+    return;
+  }
+  typedef Rec<PS> RL;
+  swr_persp_deriv_eq(p.eq + 3 * (RL::EQ_P + i), p.eq + 3 * RL::EQ_W, p.x, p.y, ddx, ddy);
+}
 
 struct RasterArgs {
   const uint32_t* status;
@@ -1219,6 +1232,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
       GpuPixel<PS> pd;
       pd.x = x;
       pd.y = y;
+      pd.eq = eq;
       pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
       build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
       sfz[f] = pd.z;
@@ -1272,6 +1286,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
         GpuPixel<PS> pd;
         pd.x = px[q];
         pd.y = py[q];
+        pd.eq = eq;
         pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
         if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
         build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);

@@ -66,10 +66,10 @@ class DeviceScene:
     def uniforms(self, target: DeviceTarget, mvp=None):
         sc = self.scene
         tex = self.texture
+        tw, th = sc.texture_wh()
         return make_uniforms(sc.mvp if mvp is None else mvp, sc.light, sc.checker, sc.width, sc.height,
-                             tex_ptr=tex.data_ptr() if tex is not None else 0,
-                             tex_w=sc.texture.shape[1] if tex is not None else 0,
-                             tex_h=sc.texture.shape[0] if tex is not None else 0,
+                             tex_ptr=tex.data_ptr() if tex is not None else 0, tex_w=tw, tex_h=th,
+                             max_aniso=sc.max_aniso,
                              color=target.color.data_ptr(), depth=target.depth.data_ptr(),
                              frag_count=target.frag_count.data_ptr() if target.frag_count is not None else 0,
                              winner=target.winner.data_ptr() if target.winner is not None else 0)

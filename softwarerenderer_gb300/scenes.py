@@ -46,6 +46,15 @@ class Scene:
     light: np.ndarray = field(default_factory=lambda: np.array([0, 0, 1, 0.15], np.float32))
     checker: int = 16
     texture: Optional[np.ndarray] = None
+    tex_size: Optional[Tuple[int, int]] = None  # (w, h) of level 0 when `texture` is a mip chain
+    max_aniso: int = 0                          # mip-mapped sampler's anisotropy limit (0 = 8)
+
+    def texture_wh(self):
+        if self.tex_size is not None:
+            return int(self.tex_size[0]), int(self.tex_size[1])
+        if self.texture is None:
+            return 0, 0
+        return int(self.texture.shape[1]), int(self.texture.shape[0])
 
     @property
     def rgba32f(self) -> bool:
@@ -184,6 +193,75 @@ def cube_scene(frame: int = 0, seed: int = 1) -> Scene:
                  cull=CullMode.CW, raster=RasterMode.Span, viewport=(0, 0, 640, 480),
                  scissor=(0, 0, 640, 480), attribs=[(v, 20)], indices=i, mvp=mvp,
                  texture=checker_texture())
+
+
+def rgb_texture(w: int, h: int, seed: int = 7):
+    """0x00RRGGBB texels (the SDL surface format of the reference's example texture): a
+    checker of seeded colours with per-texel ramps, so every mip level differs."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.uint32)
+    sq = max(2, min(w, h) // 8)
+    col = rng.integers(0, 256, (2, 3)).astype(np.uint32)
+    on = ((x // sq + y // sq) & 1).astype(bool)
+    r = np.where(on, col[0, 0], col[1, 0]) ^ (x & 31)
+    g = np.where(on, col[0, 1], col[1, 1]) ^ (y & 31)
+    b = np.where(on, col[0, 2], col[1, 2]) ^ ((x + y) & 15)
+    return ((r << 16) | (g << 8) | b).astype(np.uint32)
+
+
+def mip_chain(tex: np.ndarray) -> np.ndarray:
+    """Level 0 (alpha cleared) followed by every 2x2 box-filtered level down to 1x1, each
+    max(1, w // 2) x max(1, h // 2) (Texture::generateMipmaps, Texture.h:220-293); edge
+    texels of odd sizes repeat the top-left texel as the reference does."""
+    lv = np.asarray(tex, dtype=np.uint32) & np.uint32(0x00FFFFFF)
+    out = [lv.reshape(-1)]
+    h, w = lv.shape
+    while w > 1 or h > 1:
+        nw, nh = max(1, w // 2), max(1, h // 2)
+        y, x = np.mgrid[0:nh, 0:nw]
+        p00 = lv[2 * y, 2 * x]
+        p10 = np.where(2 * x + 1 < w, lv[2 * y, np.minimum(2 * x + 1, w - 1)], p00)
+        p01 = np.where(2 * y + 1 < h, lv[np.minimum(2 * y + 1, h - 1), 2 * x], p00)
+        p11 = np.where((2 * x + 1 < w) & (2 * y + 1 < h),
+                       lv[np.minimum(2 * y + 1, h - 1), np.minimum(2 * x + 1, w - 1)], p00)
+        ch = [((p00 >> s) & 255) + ((p10 >> s) & 255) + ((p01 >> s) & 255) + ((p11 >> s) & 255)
+              for s in (16, 8, 0)]
+        lv = (((ch[0] >> 2) << 16) | ((ch[1] >> 2) << 8) | (ch[2] >> 2)).astype(np.uint32)
+        out.append(lv.reshape(-1))
+        w, h = nw, nh
+    return np.concatenate(out).astype(np.uint32)
+
+
+BOX_TEXTURES = ((256, 256), (512, 128), (64, 64), (1024, 512))
+
+
+def box_scene(frame: int = 0, seed: int = 1) -> Scene:
+    """The reference's Box example (Box.cpp): the textured cube drawn in Span mode without
+    depth test through a mip-mapped anisotropic sampler fed by perspective-correct
+    derivatives, 640x480, CullMode CW.  The frame picks a seeded rotation, a camera
+    distance in {3, 5, 7, 9} and one of BOX_TEXTURES."""
+    rng = np.random.default_rng(seed)
+    rots = [random_rotation(rng) for _ in range(frame + 1)]
+    d = 3.0 + 2.0 * (frame % 4)
+    mvp = mat_to_f32(_matmul4(perspective(4.0 / 3.0, 0.1, 10.0), _matmul4(translate(0.0, 0.0, -d), rots[frame])))
+    v, i = cube_mesh()
+    tw, th = BOX_TEXTURES[frame % len(BOX_TEXTURES)]
+    return Scene(name=f"box[{frame}]", vs=VS.POS_UV, ps=PS.TEX_MIP, width=640, height=480,
+                 cull=CullMode.CW, raster=RasterMode.Span, viewport=(0, 0, 640, 480),
+                 scissor=(0, 0, 640, 480), attribs=[(v, 20)], indices=i, mvp=mvp,
+                 texture=mip_chain(rgb_texture(tw, th, seed=frame)), tex_size=(tw, th),
+                 max_aniso=(0, 4, 16, 1)[frame % 4])
+
+
+def deriv_scene(frame: int = 0, seed: int = 1, raster: RasterMode = RasterMode.Span) -> Scene:
+    """The cube with the derivative-writing shader (du/dx, du/dy, dv/dx, dv/dy as RGBA32F,
+    depth-tested): PixelData::computePerspectiveDerivatives on every covered pixel."""
+    sc = box_scene(frame, seed)
+    sc.name = f"deriv[{frame}]"
+    sc.ps = PS.PERSP_DERIV
+    sc.raster = raster
+    sc.texture, sc.tex_size, sc.max_aniso = None, None, 0
+    return sc
 
 
 # ----------------------------------------------------------------------------
@@ -470,6 +548,10 @@ def scene_from_spec(spec: dict) -> Scene:
                           raster=RasterMode(spec.get("raster", 2)))
     if k == "benchmark":
         return benchmark_scene(spec.get("n", 4096 * 10))
+    if k == "box":
+        return box_scene(spec["frame"])
+    if k == "deriv":
+        return deriv_scene(spec["frame"], raster=RasterMode(spec.get("raster", 0)))
     raise ValueError(k)
 
 
@@ -488,6 +570,8 @@ def scene_digest(scene: Scene) -> str:
                    int(scene.cull), int(scene.raster), tuple(scene.viewport),
                    tuple(float(x) for x in scene.depth_range), tuple(scene.scissor),
                    scene.checker)).encode())
+    if scene.tex_size is not None or scene.max_aniso:
+        h.update(repr((scene.texture_wh(), scene.max_aniso)).encode())
     return h.hexdigest()[:32]
 
 

@@ -35,6 +35,9 @@ def specs():
             for m in (0, 1, 2)]
     out += [{"kind": "soup", "n": 1 << 16}, {"kind": "soup", "n": 1 << 20}]
     out += [{"kind": "benchmark"}]
+    # the Box example's mip-mapped anisotropic sampler, and the perspective derivatives
+    out += [{"kind": "box", "frame": f} for f in range(16)]
+    out += [{"kind": "deriv", "frame": f, "raster": m} for f in range(8) for m in (0, 1, 2)]
     return out
 
 
