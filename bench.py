@@ -127,11 +127,19 @@ def cpu_baseline(min_seconds=10.0, max_frames=32):
         results[threads] = (frags / t_tot / 1e9, n, t_tot, 327680 * n / t_tot / 1e6)
     best = max(results, key=lambda k: results[k][0])
     v, n, t, mtris = results[best]
+    # the reference's Benchmark.cpp program: one drawElements of its scene, wall time
+    bsc = scenes.benchmark_scene()
+    btg = scenes.Target(bsc, aux=False)
+    t0 = time.perf_counter()
+    bst = port.draw(bsc, btg, threads=ncores)
+    bms = (time.perf_counter() - t0) * 1e3
     return {"value": v, "unit": "Gfrags/s", "cores": best, "kind": "port",
             "sample": f"{n} of the 32 poses, {t:.1f} s of CPU time at {best} thread(s) "
                       f"(best of 1 and {ncores} threads; OpenMP as in the reference)",
             "mtris_per_s": mtris,
-            "by_threads": {str(k): round(r[0], 4) for k, r in results.items()}}
+            "by_threads": {str(k): round(r[0], 4) for k, r in results.items()},
+            "benchmark_program": {"ms": round(bms, 1), "threads": ncores, "fragments": int(bst["fragments"]),
+                                  "gfrags_per_s": round(bst["fragments"] / (bms / 1e3) / 1e9, 4)}}
 
 
 def run_reference(args, rank):
@@ -192,8 +200,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-rendering section")
+    ap.add_argument("--section", default="all", choices=["all", "batch", "diff", "benchmark_program", "soup"],
+                    help="run one side section alone and print its JSON (profiling); 'all' is the bench line")
     args = ap.parse_args()
     assert args.warmup >= 3, "at least 3 warm-up steps"
+    if args.section != "all":
+        import torch
+        from softwarerenderer_gb300 import build
+        if not os.path.exists(build.LIB):
+            build.build()
+        fn = {"batch": run_batched, "diff": run_diff, "benchmark_program": run_benchmark_program,
+              "soup": run_soup}[args.section]
+        print(json.dumps(fn(torch, steps=args.steps)))
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -303,6 +322,8 @@ def main():
     diffr = None
     if not args.no_diff:
         diffr = run_diff(torch)
+    bprog = run_benchmark_program(torch)
+    soup = run_soup(torch)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -323,7 +344,7 @@ def main():
                 "gpu_launches": int(st["launches"]),
                 "roofline": roofline, "frame_roofline": frame_roof,
                 "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched,
-                "differentiable": diffr}
+                "differentiable": diffr, "benchmark_program": bprog, "soup_4k": soup}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -368,6 +389,79 @@ def run_batched(torch, n=256, steps=10):
     res["speedup_vs_loop"] = round(res["batch_views_per_s"] / res["loop_views_per_s"], 3)
     res["batch_mtris_per_s"] = round(res["triangles_per_step"] / (res["batch_ms_per_step"] / 1e3) / 1e6, 1)
     return res
+
+
+def run_soup(torch, steps=5, warmup=3):
+    """The triangle-soup stress configuration: 1,048,576 independent triangles at 3840x2160,
+    Adaptive mode, per-vertex RGB with depth test; about a third cross the near, far or
+    guard planes and half are culled by winding.  One drawElements per step, CUDA events,
+    256 MiB L2 flush before each step."""
+    from softwarerenderer_gb300 import scenes
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+    sc = scenes.soup_scene()
+    ds, tg = DeviceScene(sc), DeviceTarget(sc, aux=False)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    st = None
+    for _ in range(warmup):
+        tg.clear()
+        st = ds.draw(tg)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        tg.clear()
+        flush.fill_(k)
+        ev[k][0].record()
+        ds.draw(tg, sync=False)
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    rc, st2 = ds.rast.ctx.finish()
+    assert rc == 0, rc
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    frags, passes = st2["fragments"] / steps, st2["passes"] / steps
+    n_idx = len(sc.indices)
+    algo = frame_bytes(n_idx, 24 * n_idx, sc.width * sc.height, frags, passes)
+    hbm, _ = peaks()
+    return {"workload": "1,048,576-triangle soup, 3840x2160, Adaptive, depth-tested vertex colour",
+            "fragments": int(frags), "depth_passes": int(passes), "primitives": int(st["primitives"]),
+            "ms": round(ms, 4), "gfrags_per_s": round(frags / (ms / 1e3) / 1e9, 2),
+            "mtris_per_s": round(1048576 / (ms / 1e3) / 1e6, 1),
+            "frame_roofline": {"bytes_per_frame": int(algo), "achieved_gbs": round(algo / (ms / 1e3) / 1e9, 1),
+                               "peak": hbm, "frac": round(algo / (ms / 1e3) / 1e9 / hbm, 4)}}
+
+
+def run_benchmark_program(torch, steps=10, warmup=3):
+    """The reference's Benchmark.cpp program on the GPU: its scene (40,960 triangles of
+    vertices from Random(0), CullMode None, Span, 640x480, affine colour without depth test;
+    240 M fragments) drawn by one drawElements per step, each step timed with CUDA events
+    after a 256 MiB L2 flush.  Algorithmic bytes per step: indices, vertex stream, the RGBA8
+    target store and one 4-byte colour write per fragment (no depth test)."""
+    from softwarerenderer_gb300 import scenes
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+    sc = scenes.benchmark_scene()
+    ds, tg = DeviceScene(sc), DeviceTarget(sc, aux=False)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    frags = 0
+    for _ in range(warmup):
+        tg.clear()
+        frags = ds.draw(tg)["fragments"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        tg.clear()
+        flush.fill_(k)
+        ev[k][0].record()
+        ds.draw(tg, sync=False)
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    rc, st = ds.rast.ctx.finish()
+    assert rc == 0, rc
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    n_idx = len(sc.indices)
+    algo = 4 * n_idx + 24 * n_idx + 4 * sc.width * sc.height + 4 * frags
+    hbm, _ = peaks()
+    return {"workload": "Benchmark.cpp scene: 40,960 triangles, Random(0) vertices, 640x480, Span, CullMode None",
+            "fragments": int(frags), "ms": round(ms, 4), "gfrags_per_s": round(frags / (ms / 1e3) / 1e9, 2),
+            "mtris_per_s": round(40960 / (ms / 1e3) / 1e6, 1),
+            "roofline": {"bound": "hbm", "algorithmic_bytes": algo, "achieved": round(algo / (ms / 1e3) / 1e9, 1),
+                         "peak": hbm, "unit": "GB/s", "frac": round(algo / (ms / 1e3) / 1e9 / hbm, 4)}}
 
 
 def run_diff(torch, steps=20, warmup=3):

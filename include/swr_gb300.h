@@ -202,6 +202,30 @@ int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad
 int swr_mip_chain_size(int width, int height, int* levels, uint64_t* texels);
 int swr_build_mip_chain(const uint32_t* base, int width, int height, uint32_t* chain, void* stream);
 
+/* OBJ ingestion: ObjData::loadFromFile + ObjData::toVertexArray of the reference's
+ * examples (src/examples/ObjData.cpp:46-199).  A mesh holds the deduplicated vertex array
+ * (8 floats per vertex: position xyz, normal xyz, texcoord uv -- ObjData::VertexArrayData)
+ * and the fan-triangulated index array, in the reference's order.  Inputs on which the
+ * reference has undefined behaviour (indices past their lists, words with more than three
+ * '/'-separated parts, empty faces) return SWR_EINVAL.  swr_obj_read copies the arrays to
+ * host memory (no GPU needed); swr_obj_upload copies them to device buffers on `stream` and
+ * waits for it.  Either array pointer may be NULL. */
+typedef struct swr_obj_mesh swr_obj_mesh;
+int swr_obj_parse(const char* text, uint64_t len, swr_obj_mesh** out);
+int swr_obj_load(const char* path, swr_obj_mesh** out);
+int swr_obj_counts(const swr_obj_mesh* mesh, uint64_t* nverts, uint64_t* nindices);
+int swr_obj_read(const swr_obj_mesh* mesh, float* vdata, int32_t* idata);
+int swr_obj_upload(const swr_obj_mesh* mesh, float* vdata, int32_t* idata, void* stream);
+int swr_obj_free(swr_obj_mesh* mesh);
+
+/* Headless presentation (replaces the SDL window surface of the reference's examples,
+ * Box.cpp:170-171, 315): writes width x height pixels -- device or host memory, row pitch
+ * == width -- as 8-bit RGB to `path`, binary PPM for a ".ppm" name, PNG for ".png". */
+#define SWR_PIXELS_RGBA8 0    /* uint32 per pixel, R in bits 0-7 (the RGBA8 built-in shaders) */
+#define SWR_PIXELS_XRGB8 1    /* uint32 0x00RRGGBB (SWR_PS_TEX_MIP, the SDL surface format) */
+#define SWR_PIXELS_RGBA32F 2  /* 4 floats per pixel, clamped to [0, 1] and rounded */
+int swr_write_image(const char* path, const void* pixels, int width, int height, int format);
+
 /* Allocation-free triangle-list draw.  No counterpart in the reference (whose CPU
  * rasterizer needs no device scratch).  It is swr_draw_list(SWR_DRAW_TRIANGLE, ...) for
  * callers that must not allocate device memory -- an application whose device memory is

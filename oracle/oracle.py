@@ -89,6 +89,13 @@ def load(which="port"):
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
             lib.oracle_diff_fd.restype = ctypes.c_int
+        if hasattr(lib, "oracle_ref_obj"):
+            lib.oracle_ref_obj.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                           ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.POINTER(ctypes.c_uint64)]
+            lib.oracle_ref_obj.restype = ctypes.c_int
+            lib.oracle_ref_random.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p]
+            lib.oracle_ref_random.restype = None
         if hasattr(lib, "oracle_log2"):
             lib.oracle_log2.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
             lib.oracle_log2.restype = None
@@ -110,6 +117,22 @@ class Oracle:
 
     def fold(self, v, a, k):
         return self.lib.oracle_fold(v, a, k)
+
+    def ref_obj(self, path):
+        """The reference's ObjData::loadFromFile(path).toVertexArray (ref library only)."""
+        nv, ni = ctypes.c_uint64(), ctypes.c_uint64()
+        self.lib.oracle_ref_obj(os.fsencode(path), None, 0, None, 0, ctypes.byref(nv), ctypes.byref(ni))
+        v = np.zeros((nv.value, 8), np.float32)
+        i = np.zeros(ni.value, np.int32)
+        self.lib.oracle_ref_obj(os.fsencode(path), v.ctypes.data, nv.value, i.ctypes.data, ni.value,
+                                ctypes.byref(nv), ctypes.byref(ni))
+        return v, i
+
+    def ref_random(self, seed, n):
+        """n values of the reference examples' Random(seed).NextDouble() (ref library only)."""
+        out = np.zeros(n, np.float64)
+        self.lib.oracle_ref_random(int(seed), int(n), out.ctypes.data)
+        return out
 
     def log2(self, x):
         """swr_log2 (the texture sampler's level-of-detail logarithm) of a float32 array."""

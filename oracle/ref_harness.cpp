@@ -169,3 +169,27 @@ extern "C" int oracle_draw(const OracleDraw* d, OracleStats* st) {
 }
 
 extern "C" float oracle_fold(float v, float a, int k) { return swr_fold(v, a, k); }
+
+// The reference examples' Random (src/examples/Random.cpp, the generator Benchmark.cpp
+// draws its vertices from): n values of NextDouble() for `seed`.
+#include "Random.h"
+extern "C" void oracle_ref_random(int seed, uint64_t n, double* out) {
+  Random r(seed);
+  for (uint64_t i = 0; i < n; ++i) out[i] = r.NextDouble();
+}
+
+// The examples' OBJ loader (src/examples/ObjData.cpp): loadFromFile + toVertexArray.
+// Returns the vertex and index counts; copies at most the given capacities.
+#include "ObjData.h"
+extern "C" int oracle_ref_obj(const char* path, float* vdata, uint64_t vcap, int32_t* idata, uint64_t icap,
+                              uint64_t* nverts, uint64_t* nidx) {
+  std::vector<ObjData::VertexArrayData> vd;
+  std::vector<int> id;
+  ObjData::loadFromFile(path).toVertexArray(vd, id);
+  static_assert(sizeof(ObjData::VertexArrayData) == 32, "8 floats per vertex");
+  *nverts = vd.size();
+  *nidx = id.size();
+  if (vdata) memcpy(vdata, vd.data(), 32 * (vd.size() < vcap ? vd.size() : vcap));
+  for (size_t i = 0; idata && i < id.size() && i < icap; ++i) idata[i] = id[i];
+  return 0;
+}

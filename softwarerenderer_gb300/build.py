@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libswr_gb300.so")
-SOURCES = ["swr_core.cu", "swr_vs.cu", "swr_ps.cu", "swr_capi.cu", "swr_noalloc.cu", "swr_backward.cu", "swr_texture.cu"]
+SOURCES = ["swr_core.cu", "swr_vs.cu", "swr_ps.cu", "swr_capi.cu", "swr_noalloc.cu", "swr_backward.cu", "swr_texture.cu", "swr_obj.cpp", "swr_image.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-ftz=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
@@ -45,7 +45,7 @@ def build(verbose=False, force=False, extra_flags=()):
     jobs = []
     for s in srcs:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT_DIR, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmd = [nvcc(), *ARCH, *FLAGS, *extra_flags, "-c", src, "-o", obj]

@@ -17,6 +17,8 @@ namespace swr {
 // largest per-draw requests (words 1..5) seen since the last finish; words 14-15 count
 // colour writes.
 constexpr int kStatusWords = 16;
+constexpr size_t kBigSortSmem = 128 * 1024;  // largest segment bitmap sorted in shared memory
+constexpr int kBigSortBlocks = 304;          // 2 per SM
 constexpr int kStickyBase = 8;
 
 __global__ void k_close_draw(uint32_t* st) {
@@ -80,6 +82,7 @@ struct swr_context {
   swr::Buffer ptv, clipv, clip_table, clip_slot, tri_flags, batch_counts, batch_base;
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
   swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
+  swr::Buffer big_cells;  // k_sort_cells -> k_sort_big: [count, cell ids...]
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
   int32_t* prim_src = nullptr;  // swr_set_primitive_source
   uint64_t prim_src_cap = 0;
@@ -170,6 +173,11 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->tile_start.ensure((size_t)(ntiles + 1) * 4 + 16);
   ok &= c->cell_count.ensure((size_t)ntiles * SWR_SEGS * 4 + 16);
   ok &= c->cell_start.ensure(((size_t)ntiles * SWR_SEGS + 1) * 4 + 16);
+  if (c->big_cells.bytes < ((size_t)ntiles * SWR_SEGS + 2) * 4) {
+    ok &= c->big_cells.ensure(((size_t)ntiles * SWR_SEGS + 2) * 4 + 16);
+    // the list length and completion counter start at zero (k_sort_big resets them)
+    ok &= c->big_cells.p && cudaMemset(c->big_cells.p, 0, 8) == cudaSuccess;
+  }
   const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64 + 2 * scan_scratch_words(ntiles * SWR_SEGS);
   ok &= c->scratch.ensure(sw * 4);
   ok &= c->draws.ensure(sizeof(SwrDrawDesc));
@@ -245,8 +253,21 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
                 cstart, ncells, seg_shift, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
                 c->tile, c->keys0.as<uint32_t>(), st, s);
   const uint32_t warps_per_block = 8;
+  // cells above 16 entries are sorted by k_sort_big with a bitmap of the segment's id
+  // range in shared memory, while that range fits in kBigSortSmem
+  const size_t bm_bytes = ((size_t)1 << seg_shift) / 8 + 16;
+  // (buffer: [list length, completion counter, cell ids...], zeroed when allocated and
+  // reset by k_sort_big's last CTA)
+  const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
+  uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
   k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
-      st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>());
+      st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
+      big);
+  if (use_big) {
+    k_sort_big<<<kBigSortBlocks, 256, bm_bytes, s>>>(st, cstart, ncells, c->cap_pairs, seg_shift,
+                                                     c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
+    c->launches += 1;
+  }
   mark(c, 4, s);
   RasterArgs ra;
   ra.status = st;
@@ -368,6 +389,9 @@ int swr_create(swr_context** out) {
   if (!out) return SWR_EINVAL;
   swr_context* c = new swr_context();
   memset(&c->u, 0, sizeof(c->u));
+  // the segment bitmaps of k_sort_big may exceed the default 48 KB of dynamic shared memory
+  cudaFuncSetAttribute(k_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBigSortSmem);
+  cudaGetLastError();
   if (!c->status.ensure(kStatusWords * 4)) {
     delete c;
     return SWR_ENOMEM;
@@ -713,7 +737,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
                         c->tris.p, c->recs.p, c->tile_count.p, c->keys0.p, c->vals0.p, c->cell_count.p,
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
-                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->stage};
+                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
   if (c->graph_mode && c->gexec && sig == c->gsig) {
     if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;

@@ -325,7 +325,7 @@ struct PsVColor {
 // final image is decided purely by primitive order (the pixel shaders of
 // Benchmark.cpp:14-26 and VertexProcessorTest / RasterizerTest).  AVar = rgb.
 struct PsVColorAffine {
-  enum { AVarCount = 3, PVarCount = 0, InterpolateZ = 0, InterpolateW = 0, HasDepth = 0 };
+  enum { AVarCount = 3, PVarCount = 0, InterpolateZ = 0, InterpolateW = 0, HasDepth = 0, Overwrite = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<false>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, false); }
@@ -584,7 +584,8 @@ SWR_HD uint32_t swr_tex_sample(const SwrUniforms& t, float u, float v, float dud
 // test, every fragment overwrites the pixel with the anisotropic sample at (u, v), its
 // footprint from the perspective-correct derivatives of u and v.  PVar = uv.
 struct PsTexMip {
-  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 0, InterpolateW = 1, HasDepth = 0, NeedsEquations = 1 };
+  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 0, InterpolateW = 1, HasDepth = 0, NeedsEquations = 1,
+         Overwrite = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<false>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, false); }
@@ -651,6 +652,18 @@ enum SwrVsId { SWR_VS_POS_UV = 1, SWR_VS_POS_NRM_UV = 2, SWR_VS_POS_RGB = 3,
 enum SwrPsId { SWR_PS_TEX_NEAREST = 1, SWR_PS_LAMBERT = 2, SWR_PS_VCOLOR = 3,
                SWR_PS_VCOLOR_AFFINE = 4, SWR_PS_LAMBERT_TEX = 5, SWR_PS_DIFF = 6,
                SWR_PS_TEX_MIP = 7, SWR_PS_PERSP_DERIV = 8 };
+
+// Pixel shaders whose apply() is frags++, writes++ and an unconditional overwrite of the
+// colour and winner: a pixel's final State after n fragments depends only on the last
+// fragment's shade() and on n, so a rasterizer may shade only that fragment.
+template <class PS, class = void>
+struct SwrOverwrite {
+  enum { value = 0 };
+};
+template <class PS>
+struct SwrOverwrite<PS, decltype((void)PS::Overwrite)> {
+  enum { value = PS::Overwrite };
+};
 
 // Pixel shaders whose shade() reads the triangle's equations (PixelData::equations) --
 // set only for triangles; the reference dereferences a null pointer for points and lines.

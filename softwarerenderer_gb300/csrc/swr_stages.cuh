@@ -823,10 +823,12 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
 
 // One warp per tile: every cell of the tile is copied to `out` in increasing primitive
 // order.  Lane c owns cell c: cells of up to 16 entries are sorted in registers by the
-// lane; larger cells are ranked by the whole warp (primitive ids are unique).
+// lane; cells of up to 64 are ranked by the whole warp (primitive ids are unique); larger
+// cells go to `big_list` for k_sort_big when it is given (its capacity is the cell count,
+// so it cannot overflow), else the warp ranks them too.
 static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* status, const uint32_t* cell_start,
                                                           uint32_t ntiles, uint32_t cap_pairs, const uint32_t* in,
-                                                          uint32_t* out) {
+                                                          uint32_t* out, uint32_t* big_list, uint32_t* big_count) {
   if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   if (cell_start[(size_t)ntiles * SWR_SEGS] > cap_pairs) return;
   const int lane = threadIdx.x & 31;
@@ -855,7 +857,10 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
     for (int i = 0; i < kSmall; ++i)
       if ((uint32_t)i < m) out[s + i] = v[i];
   }
-  uint32_t big = __ballot_sync(0xffffffffu, m > kSmall);
+  constexpr uint32_t kListed = 64;  // above this the warp rank sort below costs more than a bitmap
+  const bool listed = big_list && m > kListed;
+  if (listed) big_list[atomicAdd(big_count, 1u)] = t * SWR_SEGS + (uint32_t)lane;
+  uint32_t big = __ballot_sync(0xffffffffu, m > kSmall && !listed);
   while (big) {
     const int c = __ffs(big) - 1;
     big &= big - 1u;
@@ -870,6 +875,78 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
         for (int l = 0; l < 32; ++l) rank += __shfl_sync(0xffffffffu, w, l) < val;
       }
       if (i < cm) out[cs + rank] = val;
+    }
+  }
+}
+
+// The cells listed by k_sort_cells, one CTA per cell (persistent grid): the ids of cell
+// (tile, seg) all lie in segment seg's range [seg << shift, (seg + 1) << shift), so a
+// bitmap of that range in shared memory (only the words between the cell's smallest and
+// largest id are touched) sorts them: set one bit per id, prefix-count the words, write
+// the set bits out in order.  Dynamic shared memory: (1 << shift) / 8 bytes.
+// big_count[0] is the list length, big_count[1] a CTA completion counter: the last CTA to
+// finish resets both to zero for the next draw (they start zeroed).
+static __global__ void __launch_bounds__(256) k_sort_big(const uint32_t* status, const uint32_t* cell_start,
+                                                        uint32_t ncells, uint32_t cap_pairs, int seg_shift,
+                                                        const uint32_t* in, uint32_t* out,
+                                                        const uint32_t* big_list, uint32_t* big_count) {
+  extern __shared__ uint32_t bm[];
+  __shared__ uint32_t lohi[2];
+  __shared__ uint32_t tmp[32];
+  const bool skip = (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) || cell_start[ncells] > cap_pairs;
+  const uint32_t nbig = skip ? 0u : min(*(volatile uint32_t*)big_count, ncells);
+  const uint32_t R = 1u << seg_shift;
+  for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const uint32_t cell = big_list[bi];
+    if (cell >= ncells) continue;  // uniform per CTA
+    const uint32_t s = cell_start[cell], e = cell_start[cell + 1];
+    const uint32_t m = (e >= s && e <= cap_pairs) ? e - s : 0u;
+    const uint32_t lo_id = (cell % SWR_SEGS) << seg_shift;
+    if (threadIdx.x == 0) {
+      lohi[0] = 0xffffffffu;
+      lohi[1] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+      const uint32_t v = in[s + j] - lo_id;
+      if (v < R) {
+        atomicMin(&lohi[0], v);
+        atomicMax(&lohi[1], v);
+      }
+    }
+    __syncthreads();
+    const uint32_t lo = lohi[0], hi = lohi[1];
+    const bool any = lo <= hi;
+    const uint32_t w0 = any ? lo >> 5 : 0u, nw = any ? (hi >> 5) - w0 + 1 : 0u;
+    for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) bm[w0 + w] = 0u;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+      const uint32_t v = in[s + j] - lo_id;
+      if (v < R) atomicOr(&bm[v >> 5], 1u << (v & 31));
+    }
+    __syncthreads();
+    // thread t owns words [w0 + t * per, w0 + (t + 1) * per)
+    const uint32_t per = (nw + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = min(nw, threadIdx.x * per), b = min(nw, a + per);
+    uint32_t cnt = 0;
+    for (uint32_t w = a; w < b; ++w) cnt += __popc(bm[w0 + w]);
+    uint32_t pos = swr_block_exscan(cnt, tmp, nullptr);
+    for (uint32_t w = a; w < b; ++w) {
+      uint32_t bits = bm[w0 + w];
+      while (bits) {
+        const int bit = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        if (pos < m) out[s + pos] = lo_id + ((w0 + w) << 5) + (uint32_t)bit;
+        ++pos;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&big_count[1], 1u) == gridDim.x - 1) {
+      big_count[0] = 0u;
+      big_count[1] = 0u;
     }
   }
 }
@@ -1252,6 +1329,27 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
         hits |= (uint64_t)__ballot_sync(0xffffffffu, h) << k0;
       }
       const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+      uint32_t extra = 0;  // overwrite shaders: covering fragments before the last one
+      if (SwrOverwrite<PS>::value) {
+        // only the chunk's last covering primitive shades; the others only count
+        int last = -1;
+        uint32_t cnt = 0;
+        while (hits) {
+          const int k = __ffsll((long long)hits) - 1;
+          hits &= hits - 1ull;
+          if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
+            ++cnt;
+            last = k;
+          }
+        }
+        if (cnt) {
+          hits = 1ull << last;
+          extra = cnt - 1;
+          frags += extra;
+          st[q].frags += extra;
+          st[q].writes += extra;
+        }
+      }
       while (hits) {
         const int k = __ffsll((long long)hits) - 1;
         hits &= hits - 1ull;

@@ -264,6 +264,32 @@ def deriv_scene(frame: int = 0, seed: int = 1, raster: RasterMode = RasterMode.S
     return sc
 
 
+def icosphere_obj_text(level: int = 3) -> bytes:
+    """An OBJ file of the unit icosphere: v, vn (= position), vt (planar), faces v/t/n."""
+    p, f = icosphere(level)
+    out = ["# icosphere level %d" % level]
+    out += ["v %.7g %.7g %.7g" % tuple(x) for x in p]
+    out += ["vn %.7g %.7g %.7g" % tuple(x) for x in p]
+    out += ["vt %.7g %.7g" % ((x[0] + 1.0) * 0.5, (x[1] + 1.0) * 0.5) for x in p]
+    out += ["f " + " ".join("%d/%d/%d" % (k + 1, k + 1, k + 1) for k in tri) for tri in f]
+    return ("\n".join(out) + "\n").encode()
+
+
+def obj_scene(vdata: np.ndarray, idata: np.ndarray, pose: int = 0, width: int = 640, height: int = 480,
+              raster: RasterMode = RasterMode.Block) -> Scene:
+    """A mesh loaded from OBJ (vertex records {position, normal, texcoord}, 32 B) drawn
+    with the Lambert shader: stream 0 reads position + normal, stream 1 the texcoord of
+    the same records (offset 24 B, stride 32 B)."""
+    rot, d, _ = sphere_poses(2)[pose]
+    mvp = mat_to_f32(_matmul4(perspective(width / height, 0.1, 100.0), _matmul4(translate(0.0, 0.0, -d), rot)))
+    v = np.ascontiguousarray(vdata, dtype=np.float32).reshape(-1)
+    l = normalized([0.3, 0.5, 0.8])
+    return Scene(name=f"obj[{pose}]", vs=VS.POS_NRM_UV, ps=PS.LAMBERT, width=width, height=height,
+                 cull=CullMode.CW, raster=raster, viewport=(0, 0, width, height), scissor=(0, 0, width, height),
+                 attribs=[(v, 32), (v[6:], 32)], indices=np.asarray(idata, dtype=np.int32), mvp=mvp,
+                 light=np.array([l[0], l[1], l[2], 0.15], np.float32), checker=8)
+
+
 # ----------------------------------------------------------------------------
 # config: dense icosphere, 1920x1080, Block
 
@@ -517,14 +543,64 @@ def random_scene(seed: int, direct: Optional[bool] = None, draw_mode: Optional[D
 # ----------------------------------------------------------------------------
 # Benchmark.cpp-shaped scene and spec-driven construction (fixtures, tests, bench)
 
+class SubtractiveRandom:
+    """Knuth's subtractive generator (The Art of Computer Programming, vol. 2, 3.6) in the
+    form of .NET's System.Random, which the reference's examples/Random.cpp reproduces:
+    a 55-entry lagged table seeded from MSEED - |seed|, shuffled four times, then
+    x[n] = x[n-55] - x[n-24] mod (2^31 - 1); next_double() = sample / (2^31 - 1)."""
+
+    MBIG = 2147483647
+    MSEED = 161803398
+
+    @staticmethod
+    def _i32(x: int) -> int:  # 32-bit two's-complement wrap of the C++ int arithmetic
+        return (x + 2147483648) % 4294967296 - 2147483648
+
+    def __init__(self, seed: int = 0):
+        w, mbig = self._i32, self.MBIG
+        sub = mbig if seed == -2147483648 else abs(seed)
+        t = [0] * 56
+        mj = w(self.MSEED - sub)
+        t[55] = mj
+        mk = 1
+        for i in range(1, 55):
+            ii = (21 * i) % 55
+            t[ii] = mk
+            mk = w(mj - mk)
+            if mk < 0:
+                mk = w(mk + mbig)
+            mj = t[ii]
+        for _ in range(1, 5):
+            for i in range(1, 56):
+                t[i] = w(t[i] - t[1 + (i + 30) % 55])
+                if t[i] < 0:
+                    t[i] = w(t[i] + mbig)
+        self.t, self.inext, self.inextp = t, 0, 21
+
+    def next_int(self) -> int:
+        w = self._i32
+        self.inext = self.inext + 1 if self.inext + 1 < 56 else 1
+        self.inextp = self.inextp + 1 if self.inextp + 1 < 56 else 1
+        r = w(self.t[self.inext] - self.t[self.inextp])
+        if r == self.MBIG:
+            r -= 1
+        if r < 0:
+            r = w(r + self.MBIG)
+        self.t[self.inext] = r
+        return r
+
+    def next_doubles(self, n: int) -> np.ndarray:
+        """n values of next_double(), i.e. next_int() * (1.0 / (2^31 - 1)) in binary64."""
+        scale = 1.0 / self.MBIG
+        return np.array([self.next_int() for _ in range(n)], dtype=np.float64) * scale
+
+
 def benchmark_scene(n_tris: int = 4096 * 10, seed: int = 0) -> Scene:
-    """The shape of the reference's own benchmark scene (Benchmark.cpp:66-105): 40,960
-    triangles of three fresh vertices each with x, y, z and r, g, b uniform in [0, 1), w = 1
-    (identity transform), 640x480 viewport and scissor, CullMode None, default Span mode,
-    an affine-colour pixel shader without depth test.  Values come from numpy's PCG64
-    rather than the reference's Random class."""
-    rng = np.random.default_rng(seed)
-    v = rng.random((3 * n_tris, 6)).astype(np.float32)
+    """The reference's own benchmark scene (Benchmark.cpp:66-105): 40,960 triangles of three
+    fresh vertices each, x, y, z, r, g, b = (float)Random(0).NextDouble() in that order,
+    w = 1 (identity transform), 640x480 viewport and scissor, CullMode None, default Span
+    mode, an affine-colour pixel shader without depth test."""
+    v = SubtractiveRandom(seed).next_doubles(3 * n_tris * 6).astype(np.float32).reshape(3 * n_tris, 6)
     return Scene(name=f"benchmark{n_tris}", vs=VS.POS_RGB_AFFINE, ps=PS.VCOLOR_AFFINE, width=640,
                  height=480, cull=CullMode.None_, raster=RasterMode.Span, viewport=(0, 0, 640, 480),
                  scissor=(0, 0, 640, 480), attribs=[(v, 24)],
