@@ -37,6 +37,9 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
             "test, 32 seeded poses (3 near-plane clipped), 1 frame per step")
 
 
+NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 21421568}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -200,6 +203,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-rendering section")
+    ap.add_argument("--no-program", action="store_true", help="skip the Benchmark.cpp program section")
+    ap.add_argument("--no-soup", action="store_true", help="skip the 4K triangle-soup section")
     ap.add_argument("--section", default="all", choices=["all", "batch", "diff", "benchmark_program", "soup"],
                     help="run one side section alone and print its JSON (profiling); 'all' is the bench line")
     args = ap.parse_args()
@@ -298,12 +303,9 @@ def main():
     alg = per_launch.get(dom, 0)
     t_launch = stages[dom] / args.steps / 1e3
     achieved = alg / t_launch / 1e9 if t_launch > 0 else 0.0
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(dom)
-    except Exception:
-        pass
+    # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the dominant
+    # kernel on this workload, from an ncu capture of the pose-0 frame (tile 16)
+    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(dom) if args.tile == 16 else None
     roofline = {"bound": "hbm", "kernel": f"k_raster<PsLambert,{args.tile}>" if dom == "raster" else dom,
                 "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 5), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
@@ -322,8 +324,8 @@ def main():
     diffr = None
     if not args.no_diff:
         diffr = run_diff(torch)
-    bprog = run_benchmark_program(torch)
-    soup = run_soup(torch)
+    bprog = None if args.no_program else run_benchmark_program(torch)
+    soup = None if args.no_soup else run_soup(torch)
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:

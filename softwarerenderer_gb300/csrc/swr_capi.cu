@@ -3,6 +3,7 @@
 // one stream whose variable sizes (clip output, primitives, bin pairs) stay on the
 // device; overflow of a scratch queue is detected on the device, skips the raster stage
 // and is reported by swr_finish, which grows the queue for the next attempt.
+#include <algorithm>
 #include <stdio.h>
 #include <string.h>
 #include <vector>
@@ -17,15 +18,16 @@ namespace swr {
 // largest per-draw requests (words 1..5) seen since the last finish; words 14-15 count
 // colour writes.
 constexpr int kStatusWords = 16;
-constexpr size_t kBigSortSmem = 128 * 1024;  // largest segment bitmap sorted in shared memory
-constexpr int kBigSortBlocks = 304;          // 2 per SM
+constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CTA (bounds one warp's bitmap)
+constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
 constexpr int kStickyBase = 8;
 
-__global__ void k_close_draw(uint32_t* st) {
+__global__ void k_close_draw(uint32_t* st, uint32_t* big_count) {
   for (int i = SWR_ST_CLIP_SLOTS; i <= SWR_ST_FRAGS; ++i) {
     const uint32_t v = st[i];
     if (v > st[kStickyBase + i]) st[kStickyBase + i] = v;
   }
+  if (big_count) *big_count = 0u;  // the large-cell list of this draw's binning is consumed
 }
 
 struct Buffer {
@@ -253,19 +255,20 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
                 cstart, ncells, seg_shift, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
                 c->tile, c->keys0.as<uint32_t>(), st, s);
   const uint32_t warps_per_block = 8;
-  // cells above 16 entries are sorted by k_sort_big with a bitmap of the segment's id
-  // range in shared memory, while that range fits in kBigSortSmem
-  const size_t bm_bytes = ((size_t)1 << seg_shift) / 8 + 16;
-  // (buffer: [list length, completion counter, cell ids...], zeroed when allocated and
-  // reset by k_sort_big's last CTA)
+  // cells above 64 entries are sorted by k_sort_big, one warp per cell, with a bitmap of
+  // the segment's id range in shared memory, while that range fits in kBigSortSmem
+  const size_t bm_bytes = ((size_t)1 << seg_shift) / 8;  // one warp's bitmap
+  const int big_warps = (int)std::min<size_t>(8, std::max<size_t>(1, kBigSortSmem / std::max<size_t>(bm_bytes, 1)));
+  // (buffer: [list length, unused, cell ids...]; the length is zeroed when the buffer is
+  // allocated and reset by k_close_draw at the end of every draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
   k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
       st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
       big);
   if (use_big) {
-    k_sort_big<<<kBigSortBlocks, 256, bm_bytes, s>>>(st, cstart, ncells, c->cap_pairs, seg_shift,
-                                                     c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
+    k_sort_big<<<kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s>>>(
+        st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
     c->launches += 1;
   }
   mark(c, 4, s);
@@ -283,7 +286,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.status_w = st;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
-  k_close_draw<<<1, 1, 0, s>>>(st);
+  k_close_draw<<<1, 1, 0, s>>>(st, big);
   c->launches += 1 + 2 + 1 + 1 + (ntiles ? 1 : 0) + 1;
   return cuda_err(cudaGetLastError());
 }
@@ -352,7 +355,7 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
   sh.status_w = st;
   ps->lp_shade(sh, s);
   mark(c, 5, s);
-  k_close_draw<<<1, 1, 0, s>>>(st);
+  k_close_draw<<<1, 1, 0, s>>>(st, nullptr);
   c->launches += 1 + 2 + 1 + 3 * ((bits + 7) / 8) + 1 + 1;
   return cuda_err(cudaGetLastError());
 }

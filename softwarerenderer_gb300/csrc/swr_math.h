@@ -176,8 +176,8 @@ SWR_HD float swr_fold(float v, float a, int k) {
       continue;
     }
     if (Dm == 0) return v;
-    int32_t m = slack / Dm + 1;
-    if (m > k) m = k;
+    // m = min(k, slack / Dm + 1); the whole run usually fits, which needs no division
+    int32_t m = (int64_t)(k - 1) * Dm <= (int64_t)slack ? k : slack / Dm + 1;
     const int32_t N2 = grow ? N + m * Dm : N - m * Dm;
     // N2 == 2^24 carries into the exponent (and into +-inf from the top binade).
     v = swr_u2f((vb & 0x80000000u) + ((ve << 23) + (uint32_t)(N2 - 0x800000)));

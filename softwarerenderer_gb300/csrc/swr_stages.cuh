@@ -879,58 +879,59 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
   }
 }
 
-// The cells listed by k_sort_cells, one CTA per cell (persistent grid): the ids of cell
-// (tile, seg) all lie in segment seg's range [seg << shift, (seg + 1) << shift), so a
-// bitmap of that range in shared memory (only the words between the cell's smallest and
-// largest id are touched) sorts them: set one bit per id, prefix-count the words, write
-// the set bits out in order.  Dynamic shared memory: (1 << shift) / 8 bytes.
-// big_count[0] is the list length, big_count[1] a CTA completion counter: the last CTA to
-// finish resets both to zero for the next draw (they start zeroed).
-static __global__ void __launch_bounds__(256) k_sort_big(const uint32_t* status, const uint32_t* cell_start,
-                                                        uint32_t ncells, uint32_t cap_pairs, int seg_shift,
-                                                        const uint32_t* in, uint32_t* out,
-                                                        const uint32_t* big_list, uint32_t* big_count) {
-  extern __shared__ uint32_t bm[];
-  __shared__ uint32_t lohi[2];
-  __shared__ uint32_t tmp[32];
+// The cells listed by k_sort_cells, one warp per cell (grid-stride over the list): the ids
+// of cell (tile, seg) all lie in segment seg's range [seg << shift, (seg + 1) << shift), so
+// a bitmap of that range in the warp's slice of shared memory sorts them: set one bit per
+// id (only the words between the cell's smallest and largest id are touched), prefix-count
+// the words across the lanes, write the set bits out in order.  Dynamic shared memory:
+// (1 << shift) / 8 bytes per warp.  big_count[0] is the list length (reset after the draw).
+static __global__ void k_sort_big(const uint32_t* status, const uint32_t* cell_start, uint32_t ncells,
+                                  uint32_t cap_pairs, int seg_shift, const uint32_t* in, uint32_t* out,
+                                  const uint32_t* big_list, const uint32_t* big_count) {
+  extern __shared__ uint32_t smem_bm[];
   const bool skip = (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) || cell_start[ncells] > cap_pairs;
   const uint32_t nbig = skip ? 0u : min(*(volatile uint32_t*)big_count, ncells);
   const uint32_t R = 1u << seg_shift;
-  for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint32_t* bm = smem_bm + (size_t)wib * (R >> 5);
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t bi = blockIdx.x * (blockDim.x >> 5) + wib; bi < nbig; bi += nwarps) {
     const uint32_t cell = big_list[bi];
-    if (cell >= ncells) continue;  // uniform per CTA
+    if (cell >= ncells) continue;  // uniform per warp
     const uint32_t s = cell_start[cell], e = cell_start[cell + 1];
     const uint32_t m = (e >= s && e <= cap_pairs) ? e - s : 0u;
     const uint32_t lo_id = (cell % SWR_SEGS) << seg_shift;
-    if (threadIdx.x == 0) {
-      lohi[0] = 0xffffffffu;
-      lohi[1] = 0u;
-    }
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (uint32_t j = lane; j < m; j += 32) {
       const uint32_t v = in[s + j] - lo_id;
       if (v < R) {
-        atomicMin(&lohi[0], v);
-        atomicMax(&lohi[1], v);
+        lo = min(lo, v);
+        hi = max(hi, v);
       }
     }
-    __syncthreads();
-    const uint32_t lo = lohi[0], hi = lohi[1];
-    const bool any = lo <= hi;
-    const uint32_t w0 = any ? lo >> 5 : 0u, nw = any ? (hi >> 5) - w0 + 1 : 0u;
-    for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) bm[w0 + w] = 0u;
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) {
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lo > hi) continue;  // uniform: no valid id
+    const uint32_t w0 = lo >> 5, nw = (hi >> 5) - w0 + 1;
+    for (uint32_t w = lane; w < nw; w += 32) bm[w0 + w] = 0u;
+    __syncwarp();
+    for (uint32_t j = lane; j < m; j += 32) {
       const uint32_t v = in[s + j] - lo_id;
       if (v < R) atomicOr(&bm[v >> 5], 1u << (v & 31));
     }
-    __syncthreads();
-    // thread t owns words [w0 + t * per, w0 + (t + 1) * per)
-    const uint32_t per = (nw + blockDim.x - 1) / blockDim.x;
-    const uint32_t a = min(nw, threadIdx.x * per), b = min(nw, a + per);
+    __syncwarp();
+    // lane l owns words [l * per, (l + 1) * per) of the range
+    const uint32_t per = (nw + 31) / 32;
+    const uint32_t a = min(nw, (uint32_t)lane * per), b = min(nw, a + per);
     uint32_t cnt = 0;
     for (uint32_t w = a; w < b; ++w) cnt += __popc(bm[w0 + w]);
-    uint32_t pos = swr_block_exscan(cnt, tmp, nullptr);
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    uint32_t pos = inc - cnt;
     for (uint32_t w = a; w < b; ++w) {
       uint32_t bits = bm[w0 + w];
       while (bits) {
@@ -940,14 +941,7 @@ static __global__ void __launch_bounds__(256) k_sort_big(const uint32_t* status,
         ++pos;
       }
     }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(&big_count[1], 1u) == gridDim.x - 1) {
-      big_count[0] = 0u;
-      big_count[1] = 0u;
-    }
+    __syncwarp();
   }
 }
 
@@ -1073,25 +1067,20 @@ template <class PS>
 __device__ __forceinline__ void build_pixel(const float* eq, bool blockmode, float fx, float fy, int ka, int kb,
                                             GpuPixel<PS>& pd) {
   typedef Rec<PS> RL;
+  // Block pixels step kb rows then ka columns from the block corner; Span pixels ka columns
+  // from their span start (kb == 0).  The mode is uniform per primitive (and per warp).
+  auto stepped = [&](const float* q3) {
+    const float e = swr_eval(q3[0], q3[1], q3[2], fx, fy);
+    return blockmode ? fold7(fold7(e, q3[1], kb), q3[0], ka) : swr_fold(e, q3[0], ka);
+  };
   if (RL::IW) {
-    const float* q3 = eq + 3 * RL::EQ_W;
-    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-    pd.invw = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
+    pd.invw = stepped(eq + 3 * RL::EQ_W);
     pd.w = swr_div(1.0f, pd.invw);
   }
 #pragma unroll
-  for (int i = 0; i < RL::NA; ++i) {
-    const float* q3 = eq + 3 * (RL::EQ_A + i);
-    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-    pd.avar[i] = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
-  }
+  for (int i = 0; i < RL::NA; ++i) pd.avar[i] = stepped(eq + 3 * (RL::EQ_A + i));
 #pragma unroll
-  for (int i = 0; i < RL::NP; ++i) {
-    const float* q3 = eq + 3 * (RL::EQ_P + i);
-    const float v0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-    const float pt = blockmode ? fold7(v0, q3[0], ka) : swr_fold(v0, q3[0], ka);
-    pd.pvar[i] = swr_mul(pt, pd.w);
-  }
+  for (int i = 0; i < RL::NP; ++i) pd.pvar[i] = swr_mul(stepped(eq + 3 * (RL::EQ_P + i)), pd.w);
 }
 
 template <class PS>
@@ -1099,8 +1088,9 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
   typedef Rec<PS> RL;
   if (!RL::IZ) return 0.0f;
   const float* q3 = eq + 3 * RL::EQ_Z;
-  const float z0 = fold7(swr_eval(q3[0], q3[1], q3[2], fx, fy), q3[1], kb);
-  return blockmode ? fold7(z0, q3[0], ka) : swr_fold(z0, q3[0], ka);
+  const float e = swr_eval(q3[0], q3[1], q3[2], fx, fy);
+  // Span pixels start from their own row (kb == 0); the mode is uniform per primitive
+  return blockmode ? fold7(fold7(e, q3[1], kb), q3[0], ka) : swr_fold(e, q3[0], ka);
 }
 
 // One CTA per screen tile, 256 threads.  Per chunk of CH primitives of the tile's bin:
