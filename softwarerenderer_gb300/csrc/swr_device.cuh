@@ -8,6 +8,7 @@
 #define SWR_BLOCK 8           // swr::BlockSize (IRasterizer.h:33)
 #define SWR_CLIP_REF 0x80000000u  // vertex references with this bit address the clip-vertex buffer
 #define SWR_SEGS 32               // primitive segments of the binning (cells per tile)
+#define SWR_CHUNK 64              // binned primitives the tile raster stages per chunk
 
 // Status word layout (device memory, reset by every submission).
 enum SwrStatusWord {

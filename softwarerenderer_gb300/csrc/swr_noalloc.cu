@@ -206,6 +206,7 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.tile_start = tile_start;
   ra.tile_stride = 1;
   ra.bin = vals;
+  ra.bin_raw = nullptr;  // the radix sort already ordered every tile
   ra.recs = recs;
   ra.draws = dd;
   ra.targets = dt;

@@ -5,7 +5,7 @@ namespace swr {
 namespace {
 
 constexpr int kGrid = 152 * 8;
-constexpr int kChunk = 64;  // primitives staged in shared memory per bin chunk
+constexpr int kChunk = SWR_CHUNK;  // primitives staged in shared memory per bin chunk
 
 template <class PS>
 void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {

@@ -828,14 +828,17 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
 // so it cannot overflow), else the warp ranks them too.
 static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* status, const uint32_t* cell_start,
                                                           uint32_t ntiles, uint32_t cap_pairs, const uint32_t* in,
-                                                          uint32_t* out, uint32_t* big_list, uint32_t* big_count) {
+                                                          uint32_t* out, uint32_t* big_list, uint32_t* big_count,
+                                                          uint32_t self_sorted) {
   if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   if (cell_start[(size_t)ntiles * SWR_SEGS] > cap_pairs) return;
   const int lane = threadIdx.x & 31;
   const uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (t >= ntiles) return;
-  const uint32_t s = cell_start[(size_t)t * SWR_SEGS + lane];
   const uint32_t last = cell_start[(size_t)t * SWR_SEGS + SWR_SEGS];
+  // tiles of at most `self_sorted` entries are ordered by the raster kernel itself
+  if (last - cell_start[(size_t)t * SWR_SEGS] <= self_sorted) return;  // uniform per warp
+  const uint32_t s = cell_start[(size_t)t * SWR_SEGS + lane];
   // every lane takes part in the shuffle; lane 31 then uses the next tile's first start
   const uint32_t nxt = __shfl_down_sync(0xffffffffu, s, 1);
   const uint32_t e = lane < SWR_SEGS - 1 ? nxt : last;
@@ -974,6 +977,8 @@ struct RasterArgs {
   const uint32_t* tile_start;  // bin start of tile t at tile_start[t * tile_stride] (plus the end)
   uint32_t tile_stride;        // 1 for per-tile starts, SWR_SEGS for per-(tile, segment) cells
   const uint32_t* bin;         // primitive ids, each tile's range in increasing order
+  const uint32_t* bin_raw;     // optional: the unsorted ids; tiles of <= CH entries read these
+                               // and order them in the kernel (k_sort_cells skips them)
   const float* recs;
   const SwrDrawDesc* draws;
   const SwrTargetDesc* targets;
@@ -1155,10 +1160,24 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
     if (in[q]) PS::load(st[q], px[q], py[q], U);
   }
   uint32_t frags = 0;
+  // a tile whose bin fits one chunk orders its ids here: the tile's order is increasing
+  // primitive id (cells are increasing id segments), so each id's rank is its position
+  const bool self_sort = g.bin_raw && e - b <= (uint32_t)CH;
   for (uint32_t c0 = b; c0 < e; c0 += CH) {
     const int n = (int)min((uint32_t)CH, e - c0);
     __syncthreads();
-    if (threadIdx.x < n) sids[threadIdx.x] = g.bin[c0 + threadIdx.x];
+    if (self_sort) {
+      if (threadIdx.x < n) sex[threadIdx.x] = g.bin_raw[c0 + threadIdx.x];
+      __syncthreads();
+      if (threadIdx.x < n) {
+        const uint32_t v = sex[threadIdx.x];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) rank += sex[j] < v;
+        sids[rank] = v;
+      }
+    } else if (threadIdx.x < n) {
+      sids[threadIdx.x] = g.bin[c0 + threadIdx.x];
+    }
     if (threadIdx.x == 0) snc = 0;
     __syncthreads();
     {
