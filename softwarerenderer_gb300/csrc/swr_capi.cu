@@ -265,7 +265,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
   k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
       st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
-      big, (uint32_t)SWR_CHUNK);
+      big, (uint32_t)SWR_RASTER_SORT);
   if (use_big) {
     k_sort_big<<<kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s>>>(
         st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
@@ -277,7 +277,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.tile_start = cstart;
   ra.tile_stride = SWR_SEGS;
   ra.bin = c->vals0.as<uint32_t>();
-  ra.bin_raw = c->keys0.as<uint32_t>();  // tiles of <= SWR_CHUNK entries are ordered in k_raster
+  ra.bin_raw = c->keys0.as<uint32_t>();  // tiles of <= SWR_RASTER_SORT entries are ordered in k_raster
   ra.recs = c->recs.as<float>();
   ra.draws = c->draws.as<SwrDrawDesc>();
   ra.targets = c->targets.as<SwrTargetDesc>();

@@ -9,6 +9,7 @@
 #define SWR_CLIP_REF 0x80000000u  // vertex references with this bit address the clip-vertex buffer
 #define SWR_SEGS 32               // primitive segments of the binning (cells per tile)
 #define SWR_CHUNK 64              // binned primitives the tile raster stages per chunk
+#define SWR_RASTER_SORT 512       // tiles with at most this many bin entries are ordered by k_raster
 
 // Status word layout (device memory, reset by every submission).
 enum SwrStatusWord {

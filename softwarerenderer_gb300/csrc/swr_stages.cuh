@@ -208,9 +208,13 @@ __device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, uint32
   }
   const uint32_t r[3] = {D.vbase + i0, D.vbase + i1, D.vbase + i2};
   const float* v[3] = {g.ptv + (size_t)r[0] * L::S, g.ptv + (size_t)r[1] * L::S, g.ptv + (size_t)r[2] * L::S};
-  const int m = __float_as_int(v[0][7]) | __float_as_int(v[1][7]) | __float_as_int(v[2][7]);
+  // words 4-7 of a record (16-byte aligned: S is a multiple of 4): screen x, y, z, outcode
+  float4 q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) q[k] = __ldg((const float4*)(v[k] + 4));
+  const int m = __float_as_int(q[0].w) | __float_as_int(q[1].w) | __float_as_int(q[2].w);
   if (m == 0) {
-    const int c = cull_decision(D.cull, v[0][4], v[0][5], v[1][4], v[1][5], v[2][4], v[2][5]);
+    const int c = cull_decision(D.cull, q[0].x, q[0].y, q[1].x, q[1].y, q[2].x, q[2].y);
     g.tri_flags[gp] = (uint8_t)c;
     in_kept = c & 1;
     return;
@@ -977,8 +981,9 @@ struct RasterArgs {
   const uint32_t* tile_start;  // bin start of tile t at tile_start[t * tile_stride] (plus the end)
   uint32_t tile_stride;        // 1 for per-tile starts, SWR_SEGS for per-(tile, segment) cells
   const uint32_t* bin;         // primitive ids, each tile's range in increasing order
-  const uint32_t* bin_raw;     // optional: the unsorted ids; tiles of <= CH entries read these
-                               // and order them in the kernel (k_sort_cells skips them)
+  const uint32_t* bin_raw;     // optional: the unsorted ids (cell layout, tile_stride SWR_SEGS);
+                               // tiles of <= SWR_RASTER_SORT entries order them in the kernel
+                               // (k_sort_cells skips them)
   const float* recs;
   const SwrDrawDesc* draws;
   const SwrTargetDesc* targets;
@@ -1133,6 +1138,9 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
   __shared__ uint32_t snc;
   __shared__ uint16_t spart[CH * NB];  // partially covered (primitive, block) pairs
   __shared__ uint32_t snpart;
+  __shared__ uint32_t ssorted[SWR_RASTER_SORT];  // the tile's ordered bin (self-sorted tiles)
+  __shared__ uint32_t scs[SWR_SEGS + 1];          // its cell starts relative to the bin start
+  static_assert(sizeof(srec4) >= SWR_RASTER_SORT * 4, "raw bin staging fits the record area");
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t tile = blockIdx.x;
   const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
@@ -1160,24 +1168,32 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
     if (in[q]) PS::load(st[q], px[q], py[q], U);
   }
   uint32_t frags = 0;
-  // a tile whose bin fits one chunk orders its ids here: the tile's order is increasing
-  // primitive id (cells are increasing id segments), so each id's rank is its position
-  const bool self_sort = g.bin_raw && e - b <= (uint32_t)CH;
+  // A tile of at most SWR_RASTER_SORT entries orders its own bin: the cells (increasing id
+  // segments) are contiguous, so an id's position is its cell's start plus the number of
+  // smaller ids in that cell.  The raw ids are staged in the record area (used only later).
+  const bool self_sort = g.bin_raw && e - b <= (uint32_t)SWR_RASTER_SORT;
+  if (self_sort) {
+    uint32_t* sraw = (uint32_t*)srec4;
+    const uint32_t ntot = e - b;
+    if (threadIdx.x <= SWR_SEGS) scs[threadIdx.x] = g.tile_start[(size_t)tile * SWR_SEGS + threadIdx.x] - b;
+    for (uint32_t j = threadIdx.x; j < ntot; j += 256) sraw[j] = g.bin_raw[b + j];
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < ntot; j += 256) {
+      int lo = 0, hi = SWR_SEGS - 1;  // the cell holding j: last c with scs[c] <= j
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (scs[mid] <= j) lo = mid; else hi = mid - 1;
+      }
+      const uint32_t v = sraw[j], c_end = scs[lo + 1];
+      uint32_t pos = scs[lo];
+      for (uint32_t k = scs[lo]; k < c_end; ++k) pos += sraw[k] < v;
+      ssorted[pos < ntot ? pos : 0] = v;
+    }
+  }
   for (uint32_t c0 = b; c0 < e; c0 += CH) {
     const int n = (int)min((uint32_t)CH, e - c0);
     __syncthreads();
-    if (self_sort) {
-      if (threadIdx.x < n) sex[threadIdx.x] = g.bin_raw[c0 + threadIdx.x];
-      __syncthreads();
-      if (threadIdx.x < n) {
-        const uint32_t v = sex[threadIdx.x];
-        int rank = 0;
-        for (int j = 0; j < n; ++j) rank += sex[j] < v;
-        sids[rank] = v;
-      }
-    } else if (threadIdx.x < n) {
-      sids[threadIdx.x] = g.bin[c0 + threadIdx.x];
-    }
+    if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snc = 0;
     __syncthreads();
     {
