@@ -213,6 +213,7 @@ def main():
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-rendering section")
     ap.add_argument("--no-program", action="store_true", help="skip the Benchmark.cpp program section")
     ap.add_argument("--no-soup", action="store_true", help="skip the 4K triangle-soup section")
+    ap.add_argument("--no-graph", action="store_true", help="time the frames without CUDA graph replay")
     ap.add_argument("--section", default="all", choices=["all", "batch", "diff", "benchmark_program", "soup"],
                     help="run one side section alone and print its JSON (profiling); 'all' is the bench line")
     args = ap.parse_args()
@@ -262,15 +263,18 @@ def main():
         ds.rast.setUniforms(ds.uniforms(tg, poses[k % len(poses)]))
         ds.vp.drawElements(sc.draw_mode, ds.indices.numel(), ds.indices, sync=False)
 
-    # warm-up (also grows the scratch queues to their steady-state size)
+    # warm-up (also grows the scratch queues to their steady-state size), then the same
+    # frames with graph mode on: the first one captures the draw's CUDA graph
     for k in range(args.warmup):
         frame(k)
         rc, _ = ctx.finish()
         if rc == 3:  # overflow: queues grown, run again
             frame(k)
             ctx.finish()
-    ctx.set_profiling(True)
-    ctx.stage_times()
+    ctx.set_graph_mode(not args.no_graph)
+    for k in range(args.warmup):
+        frame(k)
+        ctx.finish()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if dist:
@@ -287,8 +291,22 @@ def main():
         dist.barrier()
     rc, st = ctx.finish()
     assert rc == 0, f"draw status {rc}"
-    stages = ctx.stage_times()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    # Stage times: the same frames again, launch by launch with the library's per-stage
+    # CUDA events on the draw's stream (profiling bypasses graph replay).
+    ctx.set_profiling(True)
+    ctx.stage_times()
+    ps0, ps1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ps0.record(stream)
+    for k in range(args.steps):
+        flush.fill_(k)
+        frame(k)
+    ps1.record(stream)
+    torch.cuda.synchronize()
+    rc2, _ = ctx.finish()
+    assert rc2 == 0, f"draw status {rc2}"
+    stages = ctx.stage_times()
+    ctx.set_profiling(False)
     ms_max = ms
     frags, passes = st["fragments"], st["passes"]
     ms_max, frags_all = reduce_replicas(ms, frags, dist, "cuda")
@@ -347,10 +365,12 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded icosphere and poses)",
                 "config": {"workload": WORKLOAD, "tile": args.tile, "parallelism": f"replicas x{world}",
-                           "l2": "flushed before every timed frame (256 MiB write)"},
+                           "l2": "flushed before every timed frame (256 MiB write)",
+                           "cuda_graph": not args.no_graph},
                 "mtris_per_s": round(mtris, 2),
                 "fragments_per_frame": frags / args.steps, "depth_passes_per_frame": passes / args.steps,
                 "stage_ms_per_frame": {k: round(v / args.steps, 4) for k, v in stages.items()},
+                "stage_pass_ms_per_frame": round(ps0.elapsed_time(ps1) / args.steps, 4),
                 "gpu_launches": int(st["launches"]),
                 "roofline": roofline, "frame_roofline": frame_roof,
                 "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched,
@@ -526,42 +546,76 @@ def run_diff(torch, steps=20, warmup=3):
 
 def run_e2e(ds, tg, sc, poses, args, torch):
     """Same frames through VertexProcessor.drawElements with host (pinned) inputs: every step
-    copies the vertex streams and indices host->device and reads the colour buffer back."""
+    copies the vertex streams and indices host->device and reads the colour buffer back.
+    Steps are pipelined the usual way for a GPU frame loop: device inputs and targets are
+    double-buffered and three streams overlap step k+1's input copy and step k-1's image
+    read-back with step k's draw.  The timed region spans all K steps on all streams."""
+    from softwarerenderer_gb300.device import DeviceTarget
     hv = [torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory() for a, _ in sc.attribs]
     hi = torch.from_numpy(np.asarray(sc.indices, np.int32)).pin_memory()
-    hout = torch.empty(tg.color.shape, dtype=tg.color.dtype).pin_memory()
-    stream = torch.cuda.current_stream()
+    tgs = [tg, DeviceTarget(sc, aux=False)]
+    hout = [torch.empty(tg.color.shape, dtype=tg.color.dtype).pin_memory() for _ in range(2)]
+    dv = [[torch.empty_like(d) for d, _ in ds.attribs] for _ in range(2)]
+    di = [torch.empty_like(ds.indices) for _ in range(2)]
+    strides = [st for _, st in ds.attribs]
+    comp, cin, cout = torch.cuda.current_stream(), torch.cuda.Stream(), torch.cuda.Stream()
     h2d = sum(t.numel() for t in hv) + hi.numel() * 4
-    d2h = hout.numel() * 4
+    d2h = hout[0].numel() * 4
+    unis = {(p, j): ds.uniforms(tgs[j], poses[p]) for p in range(len(poses)) for j in range(2)}
+    ev = {name: [torch.cuda.Event() for _ in range(2)] for name in ("in_ready", "in_free", "out_ready", "out_done")}
+    for j in range(2):
+        ev["in_free"][j].record(comp)
+        ev["out_done"][j].record(comp)
 
     def step(k):
-        for (dbuf, _), hbuf in zip(ds.attribs, hv):
-            dbuf.copy_(hbuf, non_blocking=True)
-        ds.indices.copy_(hi, non_blocking=True)
-        tg.clear()
-        ds.rast.setUniforms(ds.uniforms(tg, poses[k % len(poses)]))
-        ds.vp.drawElements(sc.draw_mode, ds.indices.numel(), ds.indices, sync=False)
-        hout.copy_(tg.color, non_blocking=True)
+        j = k & 1
+        cin.wait_event(ev["in_free"][j])
+        with torch.cuda.stream(cin):
+            for d, h in zip(dv[j], hv):
+                d.copy_(h, non_blocking=True)
+            di[j].copy_(hi, non_blocking=True)
+        ev["in_ready"][j].record(cin)
+        comp.wait_event(ev["in_ready"][j])
+        comp.wait_event(ev["out_done"][j])
+        tgs[j].clear()
+        for i, d in enumerate(dv[j]):
+            ds.vp.setVertexAttribPointer(i, strides[i], d)
+        ds.rast.setUniforms(unis[(k % len(poses), j)])
+        ds.vp.drawElements(sc.draw_mode, di[j].numel(), di[j], sync=False)
+        ev["in_free"][j].record(comp)
+        ev["out_ready"][j].record(comp)
+        cout.wait_event(ev["out_ready"][j])
+        with torch.cuda.stream(cout):
+            hout[j].copy_(tgs[j].color, non_blocking=True)
+        ev["out_done"][j].record(cout)
 
     for k in range(args.warmup):
         step(k)
+    torch.cuda.synchronize()
     ds.rast.ctx.finish()
     ds.rast.ctx.stage_times()
     s0 = torch.cuda.Event(enable_timing=True)
     e0 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    s0.record(stream)
+    s0.record(comp)
+    cin.wait_event(s0)
+    cout.wait_event(s0)
     for k in range(args.steps):
         step(k)
-    e0.record(stream)
+    comp.wait_stream(cin)
+    comp.wait_stream(cout)
+    e0.record(comp)
     torch.cuda.synchronize()
     rc, st = ds.rast.ctx.finish()
     assert rc == 0
+    # the last image read back equals the frame the pipeline drew for it
+    assert hout[(args.steps - 1) & 1].numpy().tobytes() == tgs[(args.steps - 1) & 1].color.cpu().numpy().tobytes()
+    ds.bind(tg)  # restore the single-buffer binding for later users of ds
     ms = s0.elapsed_time(e0)
     return {"value": round(st["fragments"] / (ms / 1e3) / 1e9, 4), "unit": "Gfrags/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": round(ms / args.steps, 4),
-            "mtris_per_s": round(327680 * args.steps / (ms / 1e3) / 1e6, 2)}
+            "mtris_per_s": round(327680 * args.steps / (ms / 1e3) / 1e6, 2),
+            "pipeline": "double-buffered inputs and targets, copy-in / draw / read-back streams"}
 
 
 if __name__ == "__main__":

@@ -122,7 +122,9 @@ typedef struct swr_draw_item {
 int swr_draw_batch(swr_context* ctx, const swr_draw_item* items, int n, void* stream);
 /* With graph mode on, swr_draw_batch captures its kernel sequence in a CUDA graph the first
  * time a batch layout (item count, sizes, shaders, modes) is seen and replays it for later
- * batches with the same layout; uniforms and buffer pointers are refreshed on every call. */
+ * batches with the same layout; uniforms and buffer pointers are refreshed on every call.
+ * Triangle swr_draw_elements calls then run as one-item batches (so they replay too),
+ * except while profiling is on (stage events need the launch-by-launch path). */
 int swr_set_graph_mode(swr_context* ctx, int on);
 
 /* Wait for the stream, report and reset the accumulated status. */

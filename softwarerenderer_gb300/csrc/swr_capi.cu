@@ -18,6 +18,8 @@ namespace swr {
 // largest per-draw requests (words 1..5) seen since the last finish; words 14-15 count
 // colour writes.
 constexpr int kStatusWords = 16;
+constexpr int kSingleSlots = 8;            // pinned descriptor slots of single draws
+constexpr size_t kSingleSlotBytes = 1024;  // >= sizeof(SwrDrawDesc) + sizeof(SwrTargetDesc)
 constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CTA (bounds one warp's bitmap)
 constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
 constexpr int kStickyBase = 8;
@@ -100,6 +102,10 @@ struct swr_context {
   // the last batch layout
   unsigned char* stage = nullptr;
   size_t stage_bytes = 0;
+  unsigned char* single_stage = nullptr;  // pinned ring of single-draw descriptor slots
+  cudaEvent_t single_ev[swr::kSingleSlots] = {};
+  bool single_pending[swr::kSingleSlots] = {};
+  int single_next = 0;
   cudaEvent_t stage_read = nullptr;  // recorded after the staging copies of the last batch
   bool stage_pending = false;
   bool graph_mode = false;
@@ -361,13 +367,31 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
   return cuda_err(cudaGetLastError());
 }
 
+// Descriptors of a single draw are staged in a ring of pinned slots (a copy from pageable
+// memory may block the host until the stream drains); a slot is rewritten only after the
+// copy that read it has run, so the host can queue kSingleSlots draws ahead of the GPU.
+static_assert(sizeof(SwrDrawDesc) + sizeof(SwrTargetDesc) <= kSingleSlotBytes, "descriptor slot size");
+
 int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, cudaStream_t s) {
-  const uint32_t zero = 0;
-  cudaMemcpyAsync(c->draws.p, &D, sizeof(D), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(c->targets.p, &T, sizeof(T), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(c->draw_vbase.p, &zero, 4, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(c->draw_bbase.p, &zero, 4, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(c->target_tile_base.p, &zero, 4, cudaMemcpyHostToDevice, s);
+  int rc;
+  if (!c->single_stage) {
+    if ((rc = cuda_err(cudaMallocHost((void**)&c->single_stage, kSingleSlots * kSingleSlotBytes)))) return rc;
+    for (int i = 0; i < kSingleSlots; ++i)
+      if ((rc = cuda_err(cudaEventCreateWithFlags(&c->single_ev[i], cudaEventDisableTiming)))) return rc;
+  }
+  const int slot = c->single_next;
+  c->single_next = (slot + 1) % kSingleSlots;
+  if (c->single_pending[slot] && (rc = cuda_err(cudaEventSynchronize(c->single_ev[slot])))) return rc;
+  unsigned char* h = c->single_stage + (size_t)slot * kSingleSlotBytes;
+  memcpy(h, &D, sizeof(D));
+  memcpy(h + sizeof(D), &T, sizeof(T));
+  cudaMemcpyAsync(c->draws.p, h, sizeof(D), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(c->targets.p, h + sizeof(D), sizeof(T), cudaMemcpyHostToDevice, s);
+  cudaEventRecord(c->single_ev[slot], s);
+  c->single_pending[slot] = true;
+  cudaMemsetAsync(c->draw_vbase.p, 0, 4, s);
+  cudaMemsetAsync(c->draw_bbase.p, 0, 4, s);
+  cudaMemsetAsync(c->target_tile_base.p, 0, 4, s);
   // reset the per-draw working counters (flags and fragment totals are sticky)
   cudaMemsetAsync(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 0, 5 * 4, s);
   return cuda_err(cudaGetLastError());
@@ -416,6 +440,9 @@ int swr_destroy(swr_context* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
   if (c->stage_read) cudaEventDestroy(c->stage_read);
+  if (c->single_stage) cudaFreeHost(c->single_stage);
+  for (int i = 0; i < kSingleSlots; ++i)
+    if (c->single_ev[i]) cudaEventDestroy(c->single_ev[i]);
   if (c->stage) cudaFreeHost(c->stage);
   delete c;
   return SWR_OK;
@@ -498,6 +525,30 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   if (!vs || !ps) return SWR_EINVAL;
   if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
   if (ps->needs_eq && mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // PixelData::equations is null
+  if (c->graph_mode && !c->profiling && mode == SWR_DRAW_TRIANGLE) {
+    // graph mode: the draw is a one-item batch, captured once per layout and replayed
+    swr_draw_item it;
+    memset(&it, 0, sizeof(it));
+    it.vs_id = c->vs_id;
+    it.ps_id = c->ps_id;
+    it.cull_mode = c->cull;
+    it.raster_mode = c->raster_mode;
+    it.viewport[0] = c->vp_x; it.viewport[1] = c->vp_y; it.viewport[2] = c->vp_w; it.viewport[3] = c->vp_h;
+    it.depth_range[0] = c->dn;
+    it.depth_range[1] = c->df;
+    it.scissor[0] = c->sc_x; it.scissor[1] = c->sc_y; it.scissor[2] = c->sc_w; it.scissor[3] = c->sc_h;
+    for (int a = 0; a < 8; ++a) {
+      it.attrib[a] = c->attribs[a].ptr;
+      it.attrib_stride[a] = c->attribs[a].stride;
+      it.attrib_bytes[a] = c->attribs[a].bytes;
+    }
+    it.indices = indices;
+    it.count = count;
+    it.uniforms = &c->u;
+    it.prim_src = c->prim_src;
+    it.prim_src_capacity = c->prim_src_cap;
+    return swr_draw_batch(c, &it, 1, stream);
+  }
   const uint64_t per = mode == SWR_DRAW_POINT ? 1 : (mode == SWR_DRAW_LINE ? 2 : 3);
   if (count % per || count / per >= 0x7fffffffull || (count && !indices)) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;

@@ -54,6 +54,11 @@ class Context:
                     "bin_pairs": st.bin_pairs, "clip_polygons": st.clip_polygons, "flags": st.flags,
                     "launches": st.launches, "passes": st.passes}
 
+    def set_graph_mode(self, on=True):
+        """Replay triangle draws (and batches) as CUDA graphs, captured once per layout."""
+        self.L.swr_set_graph_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib.check(self.L.swr_set_graph_mode(self.h, int(bool(on))), "set_graph_mode")
+
     def set_profiling(self, on=True):
         _lib.check(self.L.swr_set_profiling(self.h, int(bool(on))), "set_profiling")
 

@@ -49,3 +49,26 @@ def test_batch_shared_target_in_item_order(gpu_lib, port):
     # primitive ids restart per drawElements call, in the oracle and in the batch
     for k in ("color", "depth", "frag_count", "winner"):
         assert np.asarray(t.arrays()[k]).tobytes() == np.asarray(got[k]).tobytes(), k
+
+
+@pytest.mark.parametrize("kind", ["cube", "sphere5"])
+def test_graph_mode_single_draws(gpu_lib, port, kind):
+    """Triangle drawElements in graph mode run as one-item batches: the first draw captures
+    the graph, later draws (other poses, the other of two targets) replay it."""
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+    from .parity import diff, oracle_render
+    mk = (lambda k: scenes.cube_scene(k)) if kind == "cube" else (
+        lambda k: scenes.sphere_scene(k, level=5, width=640, height=360))
+    sc0 = mk(0)
+    ds = DeviceScene(sc0)
+    ds.rast.ctx.set_graph_mode(True)
+    tgs = [DeviceTarget(sc0), DeviceTarget(sc0)]
+    for k in range(6):
+        sc = mk(k)
+        tg = tgs[k & 1]
+        tg.clear()
+        st = ds.draw(tg, mvp=sc.mvp)
+        ref, rst = oracle_render(port, sc)
+        got = tg.to_host()
+        assert not diff(ref, got), (kind, k, diff(ref, got))
+        assert st["fragments"] == rst["fragments"]
