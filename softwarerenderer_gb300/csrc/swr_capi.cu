@@ -265,7 +265,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // the segment's id range in shared memory, while that range fits in kBigSortSmem
   const size_t bm_bytes = ((size_t)1 << seg_shift) / 8;  // one warp's bitmap
   const int big_warps = (int)std::min<size_t>(8, std::max<size_t>(1, kBigSortSmem / std::max<size_t>(bm_bytes, 1)));
-  // (buffer: [list length, unused, cell ids...]; the length is zeroed when the buffer is
+  // (buffer: [list length, spare, cell ids...]; the length is zeroed when the buffer is
   // allocated and reset by k_close_draw at the end of every draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
@@ -291,6 +291,10 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.ntargets = ntargets;
   ra.draw_prim_base = c->use_draw_pbase ? c->draw_pbase.as<uint32_t>() : nullptr;
   ra.status_w = st;
+  ra.ntiles = ntiles;
+  // one CTA per tile: a persistent grid pulling tiles from a counter measured no faster on
+  // the dense mesh and slower where few tiles carry the work (they gather on fewer SMs)
+  ra.tile_counter = nullptr;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
   k_close_draw<<<1, 1, 0, s>>>(st, big);

@@ -214,6 +214,8 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.ntargets = 1;
   ra.draw_prim_base = nullptr;
   ra.status_w = st;
+  ra.ntiles = ntiles;
+  ra.tile_counter = nullptr;  // one CTA per tile
   ps->raster(ra, ntiles, kTile, s);
   uint32_t h[16];
   if (cudaMemcpyAsync(h, st, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

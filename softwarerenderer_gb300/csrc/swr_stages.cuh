@@ -991,6 +991,8 @@ struct RasterArgs {
   int ntargets;
   const uint32_t* draw_prim_base;    // per draw first primitive (null: a single draw from 0)
   uint32_t* status_w;
+  uint32_t ntiles;
+  uint32_t* tile_counter;            // optional: persistent grid's next-tile counter (starts at 0)
 };
 
 // v <- fl(v + a) repeated k times for 0 <= k <= 7 (steps inside one 8x8 block), as
@@ -1141,17 +1143,36 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
   __shared__ uint32_t ssorted[SWR_RASTER_SORT];  // the tile's ordered bin (self-sorted tiles)
   __shared__ uint32_t scs[SWR_SEGS + 1];          // its cell starts relative to the bin start
   static_assert(sizeof(srec4) >= SWR_RASTER_SORT * 4, "raw bin staging fits the record area");
+  __shared__ uint32_t stile;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
-  const uint32_t tile = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t frags = 0, passes = 0;
+  // Tiles come from g.tile_counter (persistent grid: thread 0 claims the next non-empty
+  // tile in index order) or, without a counter, one tile per CTA (blockIdx.x).
+  for (uint32_t iter = 0;; ++iter) {
+  __syncthreads();  // the previous tile's shared state is no longer read
+  if (threadIdx.x == 0) {
+    uint32_t t;
+    if (g.tile_counter) {
+      do {
+        t = atomicAdd(g.tile_counter, 1u);
+      } while (t < g.ntiles && g.tile_start[(size_t)t * g.tile_stride] == g.tile_start[(size_t)(t + 1) * g.tile_stride]);
+    } else {
+      t = iter == 0 ? blockIdx.x : 0xffffffffu;
+    }
+    stile = t;
+  }
+  __syncthreads();
+  const uint32_t tile = stile;
+  if (tile >= g.ntiles) break;
   const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
-  if (b == e) return;
+  if (b == e) continue;  // uniform per CTA
   const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
   const SwrTargetDesc& T = g.targets[ti];
   const SwrUniforms& U = g.draws[T.first_draw].u;
   const uint32_t lt = tile - T.tile_base;
   const int ox = (int)(lt % (uint32_t)T.tiles_x) * TILE, oy = (int)(lt / (uint32_t)T.tiles_x) * TILE;
   // Thread -> pixels: each warp covers an 8 x 4 half block; 16 x 16 sub-tiles repeat.
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int px[PPT], py[PPT], blk[PPT];
   bool in[PPT];
   typename PS::State st[PPT];
@@ -1167,7 +1188,6 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
     in[q] = px[q] < T.width && py[q] < T.height;
     if (in[q]) PS::load(st[q], px[q], py[q], U);
   }
-  uint32_t frags = 0;
   // A tile of at most SWR_RASTER_SORT entries orders its own bin: the cells (increasing id
   // segments) are contiguous, so an id's position is its cell's start plus the number of
   // smaller ids in that cell.  The raw ids are staged in the record area (used only later).
@@ -1417,13 +1437,13 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
       }
     }
   }
-  uint32_t passes = 0;
 #pragma unroll
   for (int q = 0; q < PPT; ++q)
     if (in[q]) {
       PS::store(st[q], px[q], py[q], U);
       passes += st[q].writes;
     }
+  }  // tiles
   // fragment statistics: drawPixel calls and colour writes
   uint32_t tot, ptot;
   swr_block_exscan(frags, sfr, &tot);
