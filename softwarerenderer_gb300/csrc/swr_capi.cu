@@ -24,6 +24,32 @@ constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CT
 constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
 constexpr int kStickyBase = 8;
 
+// Descriptor upload from pinned host staging (device-accessible under unified addressing)
+// by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
+// large host<->device copy the application runs on another stream, delaying the draw.
+struct StageCopy {
+  void* dst[6];
+  const void* src[6];
+  uint32_t words[6];
+  int n;
+  void add(void* d, const void* s, size_t bytes) {
+    dst[n] = d;
+    src[n] = s;
+    words[n] = (uint32_t)(bytes / 4);
+    ++n;
+  }
+};
+constexpr int kStageCopyBlocks = 8;
+static_assert(sizeof(SwrDrawDesc) % 4 == 0 && sizeof(SwrTargetDesc) % 4 == 0, "descriptors copy as words");
+
+__global__ void k_stage_copy(const StageCopy sc) {
+  for (int k = 0; k < sc.n; ++k) {
+    const uint32_t* s = (const uint32_t*)sc.src[k];
+    uint32_t* d = (uint32_t*)sc.dst[k];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < sc.words[k]; i += gridDim.x * blockDim.x) d[i] = s[i];
+  }
+}
+
 __global__ void k_close_draw(uint32_t* st, uint32_t* big_count) {
   for (int i = SWR_ST_CLIP_SLOTS; i <= SWR_ST_FRAGS; ++i) {
     const uint32_t v = st[i];
@@ -389,8 +415,12 @@ int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, 
   unsigned char* h = c->single_stage + (size_t)slot * kSingleSlotBytes;
   memcpy(h, &D, sizeof(D));
   memcpy(h + sizeof(D), &T, sizeof(T));
-  cudaMemcpyAsync(c->draws.p, h, sizeof(D), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(c->targets.p, h + sizeof(D), sizeof(T), cudaMemcpyHostToDevice, s);
+  StageCopy sc;
+  sc.n = 0;
+  sc.add(c->draws.p, h, sizeof(D));
+  sc.add(c->targets.p, h + sizeof(D), sizeof(T));
+  k_stage_copy<<<1, 256, 0, s>>>(sc);
+  c->launches += 1;
   cudaEventRecord(c->single_ev[slot], s);
   c->single_pending[slot] = true;
   cudaMemsetAsync(c->draw_vbase.p, 0, 4, s);
@@ -816,11 +846,18 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     c->capturing = true;
   }
   int q = SWR_OK;
-  q = q ? q : cuda_err(cudaMemcpyAsync(c->draws.p, h + o_d, sizeof(SwrDrawDesc) * n, cudaMemcpyHostToDevice, s));
-  q = q ? q : cuda_err(cudaMemcpyAsync(c->targets.p, h + o_t, sizeof(SwrTargetDesc) * ntg, cudaMemcpyHostToDevice, s));
-  q = q ? q : cuda_err(cudaMemcpyAsync(c->draw_vbase.p, h + o_vb, 4 * n, cudaMemcpyHostToDevice, s));
-  q = q ? q : cuda_err(cudaMemcpyAsync(c->draw_bbase.p, h + o_bb, 4 * n, cudaMemcpyHostToDevice, s));
-  q = q ? q : cuda_err(cudaMemcpyAsync(c->target_tile_base.p, h + o_tb, 4 * ntg, cudaMemcpyHostToDevice, s));
+  {
+    StageCopy sc;
+    sc.n = 0;
+    sc.add(c->draws.p, h + o_d, sizeof(SwrDrawDesc) * n);
+    sc.add(c->targets.p, h + o_t, sizeof(SwrTargetDesc) * ntg);
+    sc.add(c->draw_vbase.p, h + o_vb, 4 * n);
+    sc.add(c->draw_bbase.p, h + o_bb, 4 * n);
+    sc.add(c->target_tile_base.p, h + o_tb, 4 * ntg);
+    k_stage_copy<<<kStageCopyBlocks, 256, 0, s>>>(sc);
+    c->launches += 1;
+    q = cuda_err(cudaGetLastError());
+  }
   // the host waits on this event before it rewrites the staging area; inside a capture
   // only an external record becomes a node the host can wait on
   q = q ? q : cuda_err(c->capturing ? cudaEventRecordWithFlags(c->stage_read, s, cudaEventRecordExternal)
