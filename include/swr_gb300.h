@@ -220,6 +220,14 @@ int swr_obj_read(const swr_obj_mesh* mesh, float* vdata, int32_t* idata);
 int swr_obj_upload(const swr_obj_mesh* mesh, float* vdata, int32_t* idata, void* stream);
 int swr_obj_free(swr_obj_mesh* mesh);
 
+/* Render-target clear (no reference counterpart: its applications clear their own
+ * buffers, e.g. Box.cpp's SDL_FillRect): fills the target named by u -- colour
+ * (color_bytes = 4 or 16 per pixel, the pattern at clear_color), depth (clear_depth) and,
+ * when present, frag_count (0) and winner (-1) -- in one kernel on `stream`.  Buffers must
+ * be 16-byte aligned (cudaMalloc is). */
+int swr_clear_target(const struct SwrUniforms* u, int color_bytes, const void* clear_color, float clear_depth,
+                     void* stream);
+
 /* Headless presentation (replaces the SDL window surface of the reference's examples,
  * Box.cpp:170-171, 315): writes width x height pixels -- device or host memory, row pitch
  * == width -- as 8-bit RGB to `path`, binary PPM for a ".ppm" name, PNG for ".png". */

@@ -32,11 +32,27 @@ class DeviceTarget:
         self.clear_color, self.clear_depth = clear_color, clear_depth
 
     def clear(self):
-        self.color.fill_(self.clear_color)
-        self.depth.fill_(self.clear_depth)
-        if self.frag_count is not None:
-            self.frag_count.zero_()
-            self.winner.fill_(-1)
+        """Colour, depth and the per-pixel records in one kernel (swr_clear_target)."""
+        import ctypes
+        from . import _lib
+        from .renderer import _stream
+        L = _lib.lib()
+        if getattr(self, "_clear_u", None) is None:
+            L.swr_clear_target.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_float,
+                                           ctypes.c_void_p]
+            L.swr_clear_target.restype = ctypes.c_int
+            h, w = self.depth.shape
+            self._clear_u = make_uniforms(np.eye(4), [0, 0, 1, 0], 0, w, h, color=self.color.data_ptr(),
+                                          depth=self.depth.data_ptr(),
+                                          frag_count=self.frag_count.data_ptr() if self.frag_count is not None else 0,
+                                          winner=self.winner.data_ptr() if self.winner is not None else 0)
+            if self.color.dtype == torch.float32:
+                self._clear_value = np.full(4, self.clear_color, np.float32)
+            else:
+                self._clear_value = np.array([int(self.clear_color) & 0xFFFFFFFF], np.uint32)
+        nbytes = self._clear_value.nbytes
+        _lib.check(L.swr_clear_target(ctypes.byref(self._clear_u), nbytes, self._clear_value.ctypes.data,
+                                      float(self.clear_depth), _stream()), "swr_clear_target")
 
     def to_host(self):
         out = {"color": self.color.cpu().numpy(), "depth": self.depth.cpu().numpy()}

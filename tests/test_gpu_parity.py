@@ -82,3 +82,27 @@ def test_random_lines_points(gpu_lib, port, seed, mode):
 def test_many_lines_points_multi_batch(gpu_lib, port, mode):
     sc = scenes.random_scene(77, direct=False, draw_mode=mode, n_prims=2600)
     _check(port, sc)
+
+
+@pytest.mark.parametrize("shape", [(480, 640), (37, 5), (1, 3), (1080, 1920)])
+@pytest.mark.parametrize("rgba32f", [False, True])
+def test_clear_target(gpu_lib, shape, rgba32f):
+    """swr_clear_target fills colour, depth, drawPixel counts and winners (odd sizes too)."""
+    import torch
+    from softwarerenderer_gb300.device import DeviceTarget
+    sc = scenes.cube_scene(0)
+    sc.height, sc.width = shape
+    if rgba32f:
+        sc.ps = scenes.PS.DIFF
+    tg = DeviceTarget(sc, clear_color=0.25 if rgba32f else 0x11223344, clear_depth=0.5)
+    for t in (tg.color, tg.depth, tg.frag_count, tg.winner):
+        t.view(torch.uint8).fill_(0xAB) if t.dtype != torch.uint8 else t.fill_(0xAB)
+    tg.clear()
+    torch.cuda.synchronize()
+    c = tg.color.cpu().numpy()
+    if rgba32f:
+        assert (c == np.float32(0.25)).all()
+    else:
+        assert (c.view(np.uint32) == 0x11223344).all()
+    assert (tg.depth.cpu().numpy() == np.float32(0.5)).all()
+    assert (tg.frag_count.cpu().numpy() == 0).all() and (tg.winner.cpu().numpy() == -1).all()
