@@ -241,7 +241,7 @@ struct PsTexNearest {
 // Lambert-lit procedural checker, depth-tested (config: dense icosphere).
 // AVar = normal, PVar = uv.
 struct PsLambert {
-  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1 };
+  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -279,7 +279,7 @@ struct PsLambert {
 
 // Lambert-lit and textured (nearest RGBA8), depth-tested (config: batched meshes).
 struct PsLambertTex {
-  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1 };
+  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -375,7 +375,7 @@ SWR_HD void swr_tex_bilinear_f32(const SwrUniforms& u, float tu, float tv, float
 // Differentiable-rendering shader: colour = vertex rgb * bilinear(texture, uv), RGBA32F
 // target, depth-tested.  PVar = {r, g, b, u, v}.
 struct PsDiff {
-  enum { AVarCount = 0, PVarCount = 5, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1 };
+  enum { AVarCount = 0, PVarCount = 5, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5 };
   typedef SwrStateRGBA32F State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) {
     const size_t i = (size_t)y * (size_t)u.width + (size_t)x;
@@ -663,6 +663,17 @@ struct SwrOverwrite {
 template <class PS>
 struct SwrOverwrite<PS, decltype((void)PS::Overwrite)> {
   enum { value = PS::Overwrite };
+};
+
+// Resident tile-raster CTAs per SM the register allocation of a shader's k_raster must
+// allow (RasterOccupancy in the shader; measured per workload, default 4).
+template <class PS, class = void>
+struct SwrRasterOccupancy {
+  enum { value = 4 };
+};
+template <class PS>
+struct SwrRasterOccupancy<PS, decltype((void)PS::RasterOccupancy)> {
+  enum { value = PS::RasterOccupancy };
 };
 
 // Pixel shaders whose shade() reads the triangle's equations (PixelData::equations) --

@@ -1119,7 +1119,8 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 //      through apply(), others by rebuilding the interpolants in place (z first: a failing
 //      depth test needs nothing else) and drawPixel().
 template <class PS, int TILE, int CH>
-__global__ void __launch_bounds__(256, 4) k_raster(RasterArgs g) {
+__global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRasterOccupancy<PS>::value)
+    k_raster(RasterArgs g) {
   typedef Rec<PS> RL;
   typedef typename PS::Color Color;
   constexpr int PPT = TILE * TILE / 256;  // pixels per thread
