@@ -1095,6 +1095,32 @@ __device__ __forceinline__ void build_pixel(const float* eq, bool blockmode, flo
   for (int i = 0; i < RL::NP; ++i) pd.pvar[i] = swr_mul(stepped(eq + 3 * (RL::EQ_P + i)), pd.w);
 }
 
+// Depth a depth-tested shader's State holds (the value its depth test compares against).
+template <class State>
+__device__ __forceinline__ float swr_state_depth(const State& s) {
+  return s.depth;
+}
+
+// Conservative depth cull of one primitive in one tile.  A covered pixel's z is the z
+// equation (a, b, c) evaluated ((a fx) + (b fy)) + c at the walk's start and then stepped k
+// times by b or a (build_z).  With u = 2^-24 and every walk coordinate |x| <= X, 0 <= y <= Y,
+// the exact plane values along the walk and the evaluation's terms are bounded by
+// Q = |a| X + |b| Y + |c|; the evaluation errs by at most 3.0001 u Q (a three-term naive
+// dot product) and each step adds at most u (Q + error so far), so for k u <= 1e-3 the
+// stepped z is within u Q (3.01 + 1.001 k) + (k + 3) 2^-149 (underflow) of the exact plane
+// value, which 2^-23 (k + 4) Q + 2^-126 bounds.  The exact plane minimum over the covered
+// pixel centres [x0, x1] x [y0, y1] is bounded from below with downward-rounded arithmetic.
+// Returns true when every covered pixel's z is >= dmax.
+__device__ __forceinline__ bool z_not_below(float a, float b, float c, float x0, float x1, float y0, float y1,
+                                            float X, float Y, int k, float dmax) {
+  if (k > 16384) return false;
+  const float q = __fadd_ru(__fadd_ru(__fmul_ru(fabsf(a), X), __fmul_ru(fabsf(b), Y)), fabsf(c));
+  if (!(q <= 0x1p100f)) return false;  // no overflow anywhere on the walk (and no NaN)
+  const float zlo = __fadd_rd(__fadd_rd(__fmul_rd(a, a >= 0.0f ? x0 : x1), __fmul_rd(b, b >= 0.0f ? y0 : y1)), c);
+  const float margin = __fadd_ru(__fmul_ru(q, __fmul_ru((float)(k + 4), 0x1p-23f)), 0x1p-126f);
+  return __fsub_rd(zlo, margin) >= dmax;
+}
+
 template <class PS>
 __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float fx, float fy, int ka, int kb) {
   typedef Rec<PS> RL;
@@ -1111,6 +1137,8 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 //      Block-mode blocks (the reference's corner test) and builds Span-mode rows from
 //      [xl, xr) (kept as each row's interpolation start); partially covered blocks are then
 //      finished by 8 lanes each, one row per lane, with the reference's stepped edge tests;
+//   C0. depth-tested shaders: primitives whose z cannot pass any depth test of the chunk
+//      (z_not_below against the tile's largest depth) are only counted;
 //   C1. small primitives (<= 64 covered pixels in the tile, up to FB fragments per chunk)
 //      are compacted: one thread per covered fragment rebuilds the stepped interpolants and
 //      evaluates the pixel shader's pure shade() at full SIMT width;
@@ -1145,6 +1173,11 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   __shared__ uint32_t scs[SWR_SEGS + 1];          // its cell starts relative to the bin start
   static_assert(sizeof(srec4) >= SWR_RASTER_SORT * 4, "raw bin staging fits the record area");
   __shared__ uint32_t stile;
+  constexpr bool kCull = SWR_DEPTH_CULL && SwrDepthCull<PS>::value;
+  __shared__ uint32_t swd[8];  // per warp: order key of the largest depth its pixels hold
+  __shared__ float sdmax;      // over the tile (+inf: some pixel holds +inf, nothing can be culled)
+  __shared__ uint32_t sculled[2];  // chunk primitives whose fragments are only counted
+  __shared__ int sminx[kCull ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
@@ -1216,7 +1249,34 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     __syncthreads();
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snc = 0;
-    __syncthreads();
+    // Tile depth bound at the chunk's start (depth-tested shaders, tiles of more than one
+    // chunk).  A tile with a pixel still at +inf can cull nothing (z is finite), which the
+    // barrier's OR tells for free; otherwise each warp reduces an order-preserving key of
+    // its largest depth (NaN depths, which every fragment fails, and pixels outside the
+    // target are ignored).
+    int tile_inf = 1;
+    bool cull_tile = false;
+    if constexpr (kCull) cull_tile = e - b > (uint32_t)CH;
+    if (cull_tile) {
+      bool my_inf = false;
+#pragma unroll
+      for (int q = 0; q < PPT; ++q) my_inf |= in[q] && swr_state_depth(st[q]) == __int_as_float(0x7f800000);
+      tile_inf = __syncthreads_or(my_inf);
+      if (!tile_inf) {
+        uint32_t key = 0;
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+          const float dq = swr_state_depth(st[q]);
+          const uint32_t u = __float_as_uint(dq);
+          const uint32_t kq = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+          if (in[q] && !swr_isnan(dq)) key = max(key, kq);
+        }
+        key = __reduce_max_sync(0xffffffffu, key);
+        if (lane == 0) swd[warp] = key;
+      }
+    } else {
+      __syncthreads();
+    }
     {
       constexpr int R4 = RL::R / 4;
       const float4* recs4 = (const float4*)g.recs;
@@ -1230,7 +1290,19 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     // B1: coverage per (primitive, block).  Fully covered / skipped blocks and Span rows are
     // finished here; partially covered Block-mode blocks are queued for B2.
     if (threadIdx.x == 0) snpart = 0;
+    if (kCull && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
     __syncthreads();
+    if (kCull && threadIdx.x == 0) {
+      float d = __int_as_float(0x7f800000);
+      if (!tile_inf) {
+        uint32_t key = swd[0];
+#pragma unroll
+        for (int w = 1; w < 8; ++w) key = max(key, swd[w]);
+        // key 0: no pixel with a usable depth -> NaN, which culls nothing
+        d = __uint_as_float((key & 0x80000000u) ? (key & 0x7fffffffu) : ~key);
+      }
+      sdmax = d;
+    }
     for (int i = threadIdx.x; i < n * NB; i += 256) {
       const int k = i / NB, j = i - k * NB;
       const float* r = srec + k * RL::R;
@@ -1247,6 +1319,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         }
       } else if (flags & 1) {
         const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+        int lmin = 0x7fffffff;
         for (int rr = 0; rr < SWR_BLOCK; ++rr) {
           const int y = by + rr;
           // the row's span does not depend on this block's x-overlap: the column-0 task
@@ -1265,9 +1338,11 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             if (any) span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
           }
           if ((j % NBX) == 0) sspan[k * TILE + (y - oy)] = sp;
+          if (kCull && sp.x < sp.y && sp.y > ox) lmin = min(lmin, sp.x);
           const int c0b = max(sp.x, bx) - bx, c1b = min(sp.y, bx + SWR_BLOCK) - bx;
           if (hit && c1b > c0b) m |= (((1ull << (c1b - c0b)) - 1ull) << c0b) << (rr * 8);
         }
+        if (kCull && (j % NBX) == 0 && lmin != 0x7fffffff) atomicMin(&sminx[k], lmin);
       }
       smask[i] = m;
     }
@@ -1296,22 +1371,65 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     __syncthreads();
     // C1 set-up: compact the small primitives' fragments (a prefix of the chunk's small
     // primitives whose fragments fit in FB)
+    // Depth-tested shaders: a primitive whose z is provably not below the largest depth of
+    // the tile's pixels at the chunk's start fails every depth test of the chunk (depths only
+    // decrease), so its fragments are only counted (scomp 2).  A tile still holding a +inf
+    // depth can cull nothing (z is finite), and skips the test.
     {
       uint32_t cnt = 0;
+      bool culled = false;
       if (threadIdx.x < n) {
-        const float* r = srec + threadIdx.x * RL::R;
-        if (__float_as_int(r[0]) & 1)
-          for (int j = 0; j < NB; ++j) cnt += __popc((uint32_t)smask[threadIdx.x * NB + j]) +
-                                              __popc((uint32_t)(smask[threadIdx.x * NB + j] >> 32));
+        const int k = threadIdx.x;
+        const float* r = srec + k * RL::R;
+        const float dmax = kCull ? sdmax : 0.0f;
+        const bool try_cull = kCull && dmax < __int_as_float(0x7f800000);
+        if (__float_as_int(r[0]) & 1) {
+          int cx0 = TILE, cx1 = -1, cy0 = TILE, cy1 = -1;  // covered pixels' box in the tile
+          for (int j = 0; j < NB; ++j) {
+            const uint64_t m = smask[k * NB + j];
+            cnt += __popc((uint32_t)m) + __popc((uint32_t)(m >> 32));
+            if (kCull && try_cull && m) {
+              uint32_t cols = (uint32_t)m | (uint32_t)(m >> 32);
+              cols |= cols >> 16;
+              cols |= cols >> 8;
+              cols &= 0xffu;
+              const int bx = (j % NBX) * SWR_BLOCK, by = (j / NBX) * SWR_BLOCK;
+              cx0 = min(cx0, bx + __ffs(cols) - 1);
+              cx1 = max(cx1, bx + 31 - __clz(cols));
+              cy0 = min(cy0, by + ((__ffsll((long long)m) - 1) >> 3));
+              cy1 = max(cy1, by + ((63 - __clzll((long long)m)) >> 3));
+            }
+          }
+          if (kCull && try_cull && cnt) {
+            // walk bounds: Block mode steps <= 7 rows then <= 7 columns inside the block;
+            // Span mode steps from the row's span start to the pixel
+            int steps = 2 * (SWR_BLOCK - 1);
+            float X = (float)(ox + cx1) + 0.5f;
+            if (!(__float_as_int(r[0]) & 2)) {
+              // every covered pixel lies in a row whose span reaches the tile
+              const int smin = sminx[k];
+              steps = max(0, ox + cx1 - smin);
+              if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
+            }
+            const float* zq = r + RL::EQ0 + 3 * RL::EQ_Z;
+            const float y1 = (float)(oy + cy1) + 0.5f;
+            culled = z_not_below(zq[0], zq[1], zq[2], (float)(ox + cx0) + 0.5f, (float)(ox + cx1) + 0.5f,
+                                 (float)(oy + cy0) + 0.5f, y1, X, y1, steps, dmax);
+          }
+        }
       }
-      const uint32_t cand = cnt <= SMALL ? cnt : 0u;
+      const uint32_t cand = cnt <= SMALL && !culled ? cnt : 0u;
       uint32_t tot;
       const uint32_t ex = swr_block_exscan(cand, sfr, &tot);
       if (threadIdx.x < n) {
-        const bool comp = cnt <= SMALL && ex + cnt <= FB;
+        const bool comp = !culled && cnt <= SMALL && ex + cnt <= FB;
         sex[threadIdx.x] = ex;
         scomp[threadIdx.x] = comp ? 1 : 0;
         if (comp && cnt) atomicMax(&snc, ex + cnt);
+      }
+      if (kCull && warp < 2 && sdmax < __int_as_float(0x7f800000)) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, culled);
+        if (lane == 0) sculled[warp] = bal;
       }
       __syncthreads();
     }
@@ -1375,6 +1493,20 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         hits |= (uint64_t)__ballot_sync(0xffffffffu, h) << k0;
       }
       const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+      if (kCull && sdmax < __int_as_float(0x7f800000)) {
+        // culled primitives' fragments fail the depth test: they are only counted, in any
+        // order (counters commute), outside the primitive-order walk
+        uint64_t ch = hits & ((uint64_t)sculled[0] | ((uint64_t)sculled[1] << 32));
+        hits &= ~ch;
+        while (ch) {
+          const int k = __ffsll((long long)ch) - 1;
+          ch &= ch - 1ull;
+          if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
+            frags++;
+            PS::earlyReject(__int_as_float(0x7f800000), st[q]);  // counts the rejected fragment
+          }
+        }
+      }
       uint32_t extra = 0;  // overwrite shaders: covering fragments before the last one
       if (SwrOverwrite<PS>::value) {
         // only the chunk's last covering primitive shades; the others only count

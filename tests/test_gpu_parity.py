@@ -106,3 +106,63 @@ def test_clear_target(gpu_lib, shape, rgba32f):
         assert (c.view(np.uint32) == 0x11223344).all()
     assert (tg.depth.cpu().numpy() == np.float32(0.5)).all()
     assert (tg.frag_count.cpu().numpy() == 0).all() and (tg.winner.cpu().numpy() == -1).all()
+
+
+def _prefilled_depth(scene, ref_depth, seed):
+    """A depth buffer holding, per 16 x 16 tile, one of the scene's own visible depths (so
+    whole primitives fall behind a tile's largest depth), with exact ties, per-pixel noise,
+    NaN and -inf pixels mixed in."""
+    rng = np.random.default_rng(seed)
+    h, w = ref_depth.shape
+    fin = ref_depth[np.isfinite(ref_depth)]
+    if fin.size == 0:
+        fin = np.array([0.5], np.float32)
+    d = np.empty((h, w), np.float32)
+    for ty in range(0, h, 16):
+        for tx in range(0, w, 16):
+            d[ty:ty + 16, tx:tx + 16] = fin[int(rng.integers(0, fin.size))]
+    noise = rng.random((h, w))
+    d[noise < 0.05] = ref_depth[noise < 0.05]                       # exact ties with a fragment
+    d[(noise >= 0.05) & (noise < 0.08)] = np.inf
+    d[(noise >= 0.08) & (noise < 0.09)] = np.nan
+    d[(noise >= 0.09) & (noise < 0.095)] = -np.inf
+    jit = (noise >= 0.5) & (noise < 0.6)
+    d[jit] = np.nextafter(d[jit], np.float32(np.inf) if seed & 1 else np.float32(-np.inf))
+    return d
+
+
+def _check_prefilled(port, sc, seed):
+    import torch
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+    first, _ = oracle_render(port, sc)
+    d = _prefilled_depth(sc, first["depth"], seed)
+    t = scenes.Target(sc)
+    t.depth[...] = d
+    rst = port.draw(sc, t)
+    ds = DeviceScene(sc)
+    tg = DeviceTarget(sc)
+    tg.depth.copy_(torch.from_numpy(d.copy()))
+    gst = ds.draw(tg)
+    got, ref = tg.to_host(), t.arrays()
+    bad = diff(ref, got)
+    assert not bad, f"{sc.name} {sc.raster.name}: " + "; ".join(describe(ref, got, k) for k in bad)
+    assert gst["fragments"] == rst["fragments"], (gst, rst)
+    return rst
+
+
+@pytest.mark.parametrize("seed", range(0, 48))
+def test_prefilled_depth_random(gpu_lib, port, seed):
+    """Depth-tested draws onto a target that already holds depths: whole primitives lie
+    behind a tile's largest depth from the first chunk on (the raster's tile depth cull)."""
+    sc = scenes.random_scene(3000 + seed, draw_mode=DrawMode.Triangle, n_prims=400)
+    _check_prefilled(port, sc, seed)
+
+
+@pytest.mark.parametrize("mode", [RasterMode.Span, RasterMode.Block, RasterMode.Adaptive])
+def test_dense_soup_all_modes(gpu_lib, port, mode):
+    """16k soup triangles on 320 x 240 (about 90 layers per pixel): many chunks per tile, most
+    primitives behind the tile's depths; also drawn over a prefilled depth buffer."""
+    sc = scenes.soup_scene(1 << 14, width=320, height=240, seed=11, raster=mode)
+    st = _check(port, sc)
+    assert st["fragments"] > 20 * 320 * 240
+    _check_prefilled(port, sc, 5)
