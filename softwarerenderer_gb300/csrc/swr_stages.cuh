@@ -1184,20 +1184,21 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   // Tiles come from g.tile_counter (persistent grid: thread 0 claims the next non-empty
   // tile in index order) or, without a counter, one tile per CTA (blockIdx.x).
   for (uint32_t iter = 0;; ++iter) {
-  __syncthreads();  // the previous tile's shared state is no longer read
-  if (threadIdx.x == 0) {
-    uint32_t t;
-    if (g.tile_counter) {
+  uint32_t tile = blockIdx.x;
+  if (g.tile_counter) {
+    __syncthreads();  // the previous tile's shared state is no longer read
+    if (threadIdx.x == 0) {
+      uint32_t t;
       do {
         t = atomicAdd(g.tile_counter, 1u);
       } while (t < g.ntiles && g.tile_start[(size_t)t * g.tile_stride] == g.tile_start[(size_t)(t + 1) * g.tile_stride]);
-    } else {
-      t = iter == 0 ? blockIdx.x : 0xffffffffu;
+      stile = t;
     }
-    stile = t;
+    __syncthreads();
+    tile = stile;
+  } else if (iter) {
+    break;
   }
-  __syncthreads();
-  const uint32_t tile = stile;
   if (tile >= g.ntiles) break;
   const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
   if (b == e) continue;  // uniform per CTA
@@ -1246,52 +1247,52 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   }
   for (uint32_t c0 = b; c0 < e; c0 += CH) {
     const int n = (int)min((uint32_t)CH, e - c0);
-    __syncthreads();
+    __syncthreads();  // the previous chunk's shared state is no longer read; ssorted is complete
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
-    if (threadIdx.x == 0) snc = 0;
+    if (threadIdx.x == 0) snpart = 0;
+    if (kCull && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
     // Tile depth bound at the chunk's start (depth-tested shaders, tiles of more than one
     // chunk).  A tile with a pixel still at +inf can cull nothing (z is finite), which the
-    // barrier's OR tells for free; otherwise each warp reduces an order-preserving key of
-    // its largest depth (NaN depths, which every fragment fails, and pixels outside the
-    // target are ignored).
+    // barrier's OR tells for free; otherwise the largest of the warps' order-preserving keys
+    // of their largest depths (NaN depths, which every fragment fails, and pixels outside
+    // the target are ignored).
     int tile_inf = 1;
     bool cull_tile = false;
-    if constexpr (kCull) cull_tile = e - b > (uint32_t)CH;
-    if (cull_tile) {
-      bool my_inf = false;
-#pragma unroll
-      for (int q = 0; q < PPT; ++q) my_inf |= in[q] && swr_state_depth(st[q]) == __int_as_float(0x7f800000);
-      tile_inf = __syncthreads_or(my_inf);
-      if (!tile_inf) {
+    bool my_inf = false;
+    if constexpr (kCull) {
+      cull_tile = e - b > (uint32_t)CH;
+      if (cull_tile) {
         uint32_t key = 0;
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
           const float dq = swr_state_depth(st[q]);
           const uint32_t u = __float_as_uint(dq);
           const uint32_t kq = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+          my_inf |= in[q] && dq == __int_as_float(0x7f800000);
           if (in[q] && !swr_isnan(dq)) key = max(key, kq);
         }
         key = __reduce_max_sync(0xffffffffu, key);
         if (lane == 0) swd[warp] = key;
       }
-    } else {
-      __syncthreads();
     }
+    // A: the chunk's setup records (ids read from the bin directly: sids is published by
+    // the barrier below)
     {
       constexpr int R4 = RL::R / 4;
       const float4* recs4 = (const float4*)g.recs;
 #pragma unroll 4
       for (int i = threadIdx.x; i < n * R4; i += 256) {
         const int k = i / R4, w = i - k * R4;
-        srec4[i] = recs4[(size_t)sids[k] * R4 + w];
+        const uint32_t id = self_sort ? ssorted[c0 - b + k] : __ldg(g.bin + c0 + k);
+        srec4[i] = recs4[(size_t)id * R4 + w];
       }
     }
-    __syncthreads();
+    if (cull_tile)
+      tile_inf = __syncthreads_or(my_inf);
+    else
+      __syncthreads();
     // B1: coverage per (primitive, block).  Fully covered / skipped blocks and Span rows are
     // finished here; partially covered Block-mode blocks are queued for B2.
-    if (threadIdx.x == 0) snpart = 0;
-    if (kCull && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
-    __syncthreads();
     if (kCull && threadIdx.x == 0) {
       float d = __int_as_float(0x7f800000);
       if (!tile_inf) {
@@ -1369,70 +1370,101 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       }
     }
     __syncthreads();
-    // C1 set-up: compact the small primitives' fragments (a prefix of the chunk's small
-    // primitives whose fragments fit in FB)
+    // C1 set-up (warps 0 and 1 measure primitives lane and lane + 32, warp 0 scans): compact
+    // the small primitives' fragments (a prefix of the chunk's small primitives whose
+    // fragments fit in FB).
     // Depth-tested shaders: a primitive whose z is provably not below the largest depth of
     // the tile's pixels at the chunk's start fails every depth test of the chunk (depths only
-    // decrease), so its fragments are only counted (scomp 2).  A tile still holding a +inf
+    // decrease), so its fragments are only counted (sculled).  A tile still holding a +inf
     // depth can cull nothing (z is finite), and skips the test.
-    {
-      uint32_t cnt = 0;
-      bool culled = false;
-      if (threadIdx.x < n) {
-        const int k = threadIdx.x;
+    if (warp < 2) {
+      const float dmax = kCull ? sdmax : 0.0f;
+      const bool try_cull = kCull && dmax < __int_as_float(0x7f800000);
+      auto prim_info = [&](int k, uint32_t& cnt, bool& culled) {
+        cnt = 0;
+        culled = false;
+        if (k >= n) return;
         const float* r = srec + k * RL::R;
-        const float dmax = kCull ? sdmax : 0.0f;
-        const bool try_cull = kCull && dmax < __int_as_float(0x7f800000);
-        if (__float_as_int(r[0]) & 1) {
-          int cx0 = TILE, cx1 = -1, cy0 = TILE, cy1 = -1;  // covered pixels' box in the tile
-          for (int j = 0; j < NB; ++j) {
-            const uint64_t m = smask[k * NB + j];
-            cnt += __popc((uint32_t)m) + __popc((uint32_t)(m >> 32));
-            if (kCull && try_cull && m) {
-              uint32_t cols = (uint32_t)m | (uint32_t)(m >> 32);
-              cols |= cols >> 16;
-              cols |= cols >> 8;
-              cols &= 0xffu;
-              const int bx = (j % NBX) * SWR_BLOCK, by = (j / NBX) * SWR_BLOCK;
-              cx0 = min(cx0, bx + __ffs(cols) - 1);
-              cx1 = max(cx1, bx + 31 - __clz(cols));
-              cy0 = min(cy0, by + ((__ffsll((long long)m) - 1) >> 3));
-              cy1 = max(cy1, by + ((63 - __clzll((long long)m)) >> 3));
-            }
-          }
-          if (kCull && try_cull && cnt) {
-            // walk bounds: Block mode steps <= 7 rows then <= 7 columns inside the block;
-            // Span mode steps from the row's span start to the pixel
-            int steps = 2 * (SWR_BLOCK - 1);
-            float X = (float)(ox + cx1) + 0.5f;
-            if (!(__float_as_int(r[0]) & 2)) {
-              // every covered pixel lies in a row whose span reaches the tile
-              const int smin = sminx[k];
-              steps = max(0, ox + cx1 - smin);
-              if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
-            }
-            const float* zq = r + RL::EQ0 + 3 * RL::EQ_Z;
-            const float y1 = (float)(oy + cy1) + 0.5f;
-            culled = z_not_below(zq[0], zq[1], zq[2], (float)(ox + cx0) + 0.5f, (float)(ox + cx1) + 0.5f,
-                                 (float)(oy + cy0) + 0.5f, y1, X, y1, steps, dmax);
+        if (!(__float_as_int(r[0]) & 1)) return;
+        int cx0 = TILE, cx1 = -1, cy0 = TILE, cy1 = -1;  // covered pixels' box in the tile
+        for (int j = 0; j < NB; ++j) {
+          const uint64_t m = smask[k * NB + j];
+          cnt += __popc((uint32_t)m) + __popc((uint32_t)(m >> 32));
+          if (kCull && try_cull && m) {
+            uint32_t cols = (uint32_t)m | (uint32_t)(m >> 32);
+            cols |= cols >> 16;
+            cols |= cols >> 8;
+            cols &= 0xffu;
+            const int bx = (j % NBX) * SWR_BLOCK, by = (j / NBX) * SWR_BLOCK;
+            cx0 = min(cx0, bx + __ffs(cols) - 1);
+            cx1 = max(cx1, bx + 31 - __clz(cols));
+            cy0 = min(cy0, by + ((__ffsll((long long)m) - 1) >> 3));
+            cy1 = max(cy1, by + ((63 - __clzll((long long)m)) >> 3));
           }
         }
+        if (kCull && try_cull && cnt) {
+          // walk bounds: Block mode steps <= 7 rows then <= 7 columns inside the block;
+          // Span mode steps from the row's span start to the pixel
+          int steps = 2 * (SWR_BLOCK - 1);
+          float X = (float)(ox + cx1) + 0.5f;
+          if (!(__float_as_int(r[0]) & 2)) {
+            // every covered pixel lies in a row whose span reaches the tile
+            const int smin = sminx[k];
+            steps = max(0, ox + cx1 - smin);
+            if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
+          }
+          const float* zq = r + RL::EQ0 + 3 * RL::EQ_Z;
+          const float y1 = (float)(oy + cy1) + 0.5f;
+          culled = z_not_below(zq[0], zq[1], zq[2], (float)(ox + cx0) + 0.5f, (float)(ox + cx1) + 0.5f,
+                               (float)(oy + cy0) + 0.5f, y1, X, y1, steps, dmax);
+        }
+      };
+      uint32_t cnt0;
+      bool cul0;
+      prim_info(threadIdx.x, cnt0, cul0);
+      if (warp == 1) {  // hand primitive lane + 32 to warp 0 through sex / scomp
+        sex[threadIdx.x] = cnt0;
+        scomp[threadIdx.x] = cul0;
       }
-      const uint32_t cand = cnt <= SMALL && !culled ? cnt : 0u;
-      uint32_t tot;
-      const uint32_t ex = swr_block_exscan(cand, sfr, &tot);
-      if (threadIdx.x < n) {
-        const bool comp = !culled && cnt <= SMALL && ex + cnt <= FB;
-        sex[threadIdx.x] = ex;
-        scomp[threadIdx.x] = comp ? 1 : 0;
-        if (comp && cnt) atomicMax(&snc, ex + cnt);
+      asm volatile("bar.sync 1, 64;" ::: "memory");  // warps 0 and 1 only
+      if (warp == 0) {
+        const uint32_t cnt1 = sex[lane + 32];
+        const bool cul1 = scomp[lane + 32] != 0;
+        const uint32_t cand0 = cnt0 <= SMALL && !cul0 ? cnt0 : 0u;
+        const uint32_t cand1 = cnt1 <= SMALL && !cul1 ? cnt1 : 0u;
+        uint32_t inc0 = cand0, inc1 = cand1;  // inclusive scans over lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y0 = __shfl_up_sync(0xffffffffu, inc0, o), y1 = __shfl_up_sync(0xffffffffu, inc1, o);
+          if (lane >= o) {
+            inc0 += y0;
+            inc1 += y1;
+          }
+        }
+        const uint32_t ex0 = inc0 - cand0, ex1 = __shfl_sync(0xffffffffu, inc0, 31) + inc1 - cand1;
+        const bool comp0 = !cul0 && cnt0 <= SMALL && ex0 + cnt0 <= FB;
+        const bool comp1 = !cul1 && cnt1 <= SMALL && ex1 + cnt1 <= FB;
+        if (lane < n) {
+          sex[lane] = ex0;
+          scomp[lane] = comp0 ? 1 : 0;
+        }
+        if (lane + 32 < n) {
+          sex[lane + 32] = ex1;
+          scomp[lane + 32] = comp1 ? 1 : 0;
+        }
+        const uint32_t hi = max(comp0 && cnt0 ? ex0 + cnt0 : 0u, comp1 && cnt1 ? ex1 + cnt1 : 0u);
+        const uint32_t nc_max = __reduce_max_sync(0xffffffffu, hi);
+        if (kCull) {
+          const uint32_t b0 = __ballot_sync(0xffffffffu, cul0), b1 = __ballot_sync(0xffffffffu, cul1);
+          if (lane == 0) {
+            sculled[0] = b0;
+            sculled[1] = b1;
+          }
+        }
+        if (lane == 0) snc = nc_max;
       }
-      if (kCull && warp < 2 && sdmax < __int_as_float(0x7f800000)) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, culled);
-        if (lane == 0) sculled[warp] = bal;
-      }
-      __syncthreads();
     }
+    __syncthreads();
     // C1: interpolate and shade the compacted fragments
     const int nc = (int)snc;
     for (int f = threadIdx.x; f < nc; f += 256) {
