@@ -102,6 +102,23 @@ __device__ __forceinline__ int swr_find_le(const uint32_t* base, int n, uint32_t
   return lo;
 }
 
+// Block-wide sums of two values per thread (blockDim.x multiple of 32, <= 1024), returned
+// to every thread.  `tmp` needs 64 words and is not reused by the caller.
+__device__ __forceinline__ void swr_block_sum2(uint32_t a, uint32_t b, uint32_t* tmp, uint32_t& sa, uint32_t& sb) {
+  a = __reduce_add_sync(0xffffffffu, a);
+  b = __reduce_add_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31) == 0) {
+    tmp[threadIdx.x >> 5] = a;
+    tmp[32 + (threadIdx.x >> 5)] = b;
+  }
+  __syncthreads();
+  sa = sb = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    sa += tmp[w];
+    sb += tmp[32 + w];
+  }
+}
+
 // Block-wide exclusive scan of one value per thread (blockDim.x multiple of 32, <= 1024).
 // `tmp` needs 32 words.  Returns the exclusive prefix; *total receives the block sum.
 __device__ __forceinline__ uint32_t swr_block_exscan(uint32_t v, uint32_t* tmp, uint32_t* total) {

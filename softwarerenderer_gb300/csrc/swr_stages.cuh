@@ -307,30 +307,22 @@ __device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uin
 
 #define SWR_HALF (SWR_BATCH_PRIMS / 2)  // triangles per assembly CTA (half a batch)
 
-// One CTA per half batch (512 triangles, 2 per thread): clip / cull and count the
-// survivors: half_counts[h] = (kept input slots, kept extra fan triangles).
+// One CTA per half batch (512 triangles, one per thread): clip / cull and count the
+// survivors: batch_counts[h] = (kept input slots, kept extra fan triangles).
 template <int A, int P>
-__global__ void __launch_bounds__(256) k_assemble_count(AssembleArgs g) {
-  __shared__ uint32_t tmp[32];
+__global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
+  __shared__ uint32_t tmp[64];
   __shared__ uint32_t sidx[3 * SWR_HALF];
   const uint32_t hb = blockIdx.x, b = hb >> 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + (hb & 1) * SWR_HALF;
   const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
-  uint32_t in_sum = 0, ex_sum = 0;
-  for (int j = 0; j < 2; ++j) {
-    const uint32_t q = threadIdx.x * 2 + j;
-    if (q < n) {
-      uint32_t ik, ek;
-      assemble_one<A, P>(g, D, p0 + q, sidx[3 * q], sidx[3 * q + 1], sidx[3 * q + 2], ik, ek);
-      in_sum += ik;
-      ex_sum += ek;
-    }
-  }
+  uint32_t ik = 0, ek = 0;
+  const uint32_t q = threadIdx.x;
+  if (q < n) assemble_one<A, P>(g, D, p0 + q, sidx[3 * q], sidx[3 * q + 1], sidx[3 * q + 2], ik, ek);
   uint32_t tin, tex;
-  swr_block_exscan(in_sum, tmp, &tin);
-  swr_block_exscan(ex_sum, tmp, &tex);
+  swr_block_sum2(ik, ek, tmp, tin, tex);
   if (threadIdx.x == 0) g.batch_counts[hb] = make_uint2(tin, tex);
 }
 
@@ -357,8 +349,9 @@ static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts,
 // batch base is the sum of the totals of the batches before it; the last batch publishes
 // the primitive count (and flags an undersized primitive queue).
 template <int A, int P>
-__global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
-  __shared__ uint32_t tmp[32];
+__global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
+  __shared__ uint32_t tmp[64];
+  __shared__ uint32_t tmps[32];
   __shared__ uint32_t sidx[3 * SWR_HALF];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t hb = blockIdx.x, b = hb >> 1, half = hb & 1;
@@ -372,10 +365,9 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
     before += c;
     if (i < 2 * D.bbase) dbefore += c;
   }
-  uint32_t base, dbase = 0;
-  swr_block_exscan(before, tmp, &base);
-  // the draw's first emitted primitive, for its primitive-source output (uniform per CTA)
-  if (D.prim_src) swr_block_exscan(dbefore, tmp, &dbase);
+  // base: the batch's first emitted primitive; dbase: the draw's (primitive-source output)
+  uint32_t base, dbase;
+  swr_block_sum2(before, dbefore, tmp, base, dbase);
   const uint2 c0 = g.batch_counts[2 * b], c1 = g.batch_counts[2 * b + 1];
   const uint32_t batch_in = c0.x + c1.x, batch_total = batch_in + c0.y + c1.y;
   // primitive ids seen by the pixel shader are per draw, as with one drawElements call each
@@ -384,25 +376,23 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
   // then every extra fan triangle (first half's, then second's)
   const uint32_t in_base = base + (half ? c0.x : 0u);
   const uint32_t ex_base = base + batch_in + (half ? c0.y : 0u);
-  uint32_t fl[2] = {0, 0}, slot[2] = {0xffffffffu, 0xffffffffu}, keep[2] = {0, 0};
-  uint32_t in_sum = 0, ex_sum = 0;
-  for (int j = 0; j < 2; ++j) {
-    const uint32_t q = threadIdx.x * 2 + j;
-    if (q < n) {
-      fl[j] = g.tri_flags[D.pbase + p0 + q];
-      if (fl[j] & 4) {
-        slot[j] = g.clip_slot[D.pbase + p0 + q];
-        if (slot[j] != 0xffffffffu) keep[j] = g.clip_table[slot[j]].keep;
-      } else {
-        keep[j] = fl[j] & 1;
-      }
-      in_sum += keep[j] & 1u;
-      ex_sum += __popc(keep[j] >> 1);
+  const uint32_t q = threadIdx.x;
+  uint32_t fl = 0, slot = 0xffffffffu, keep = 0;
+  if (q < n) {
+    fl = g.tri_flags[D.pbase + p0 + q];
+    if (fl & 4) {
+      slot = g.clip_slot[D.pbase + p0 + q];
+      if (slot != 0xffffffffu) keep = g.clip_table[slot].keep;
+    } else {
+      keep = fl & 1;
     }
   }
-  uint32_t tin, tex;
-  uint32_t rin = swr_block_exscan(in_sum, tmp, &tin) + in_base;
-  uint32_t rex = swr_block_exscan(ex_sum, tmp, &tex) + ex_base;
+  // one scan of (kept input slot, extra fan triangles) packed in 16-bit halves: at most 512
+  // and 512 * 13 per half batch, so the low half never carries
+  uint32_t tot;
+  const uint32_t ex = swr_block_exscan((keep & 1u) | ((uint32_t)__popc(keep >> 1) << 16), tmps, &tot);
+  uint32_t rin = (ex & 0xffffu) + in_base;
+  uint32_t rex = (ex >> 16) + ex_base;
   if (hb == gridDim.x - 1 && threadIdx.x == 0) {
     g.status[SWR_ST_PRIMS] = base + batch_total;
     if (base + batch_total > g.cap_prims) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
@@ -418,17 +408,15 @@ __global__ void __launch_bounds__(256) k_assemble_emit(AssembleArgs g) {
     if (k < D.prim_src_cap) D.prim_src[k] = (int32_t)src;
     else atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_SRC_OVERFLOW);
   };
-  for (int j = 0; j < 2; ++j) {
-    const uint32_t q = threadIdx.x * 2 + j;
-    if (!keep[j]) continue;
-    if (!(fl[j] & 4)) {
+  if (keep) {
+    if (!(fl & 4)) {
       uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
-      if (fl[j] & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
+      if (fl & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
       record_src(rin, p0 + q);
       g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
     } else {
       // first fan triangle in the input slot, the others after all of the batch's slots
-      const SwrClipEntry e = g.clip_table[slot[j]];
+      const SwrClipEntry e = g.clip_table[slot];
       for (int k = 0; k + 2 < e.n; ++k) {
         if (!((e.keep >> k) & 1)) continue;
         uint32_t r0 = e.ref[0], r1 = e.ref[k + 1], r2 = e.ref[k + 2];
@@ -574,10 +562,31 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
     const SwrTargetDesc& T = g.targets[D.target];
     const uint32_t rr[3] = {t.x, t.y, t.z};
     float x[3], y[3], z[3], w[3];
-    const float* vp[3];
+    float av[3][RL::NA > 0 ? RL::NA : 1], pv[3][RL::NP > 0 ? RL::NP : 1];
+    // Post-transform records (16-byte aligned): words 0-3 clip position, 4-6 screen x, y, z,
+    // then the vertex shader's avars and pvars.  Records of at most 16 words with the avars
+    // at word 8 and 0 or 3 of them (every built-in vertex shader) are read as float4s;
+    // scattered scalar reads of 9 words per vertex made the stage L1-wavefront bound.
+    const bool vec = g.S <= 16 && g.off_a == 8 && g.off_p == 8 + g.vs_a && (g.vs_a == 0 || g.vs_a == 3);
     for (int k = 0; k < 3; ++k) {
-      vp[k] = (rr[k] & SWR_CLIP_REF) ? g.clipv + (size_t)(rr[k] & ~SWR_CLIP_REF) * g.S : g.ptv + (size_t)rr[k] * g.S;
-      x[k] = vp[k][4]; y[k] = vp[k][5]; z[k] = vp[k][6]; w[k] = vp[k][3];
+      const float* vp = (rr[k] & SWR_CLIP_REF) ? g.clipv + (size_t)(rr[k] & ~SWR_CLIP_REF) * g.S
+                                               : g.ptv + (size_t)rr[k] * g.S;
+      if (vec) {
+        const float4 q0 = __ldg((const float4*)vp), q1 = __ldg((const float4*)vp + 1);
+        const float4 q2 = g.S > 8 ? __ldg((const float4*)vp + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 q3 = g.S > 12 ? __ldg((const float4*)vp + 3) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float at[8] = {q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+        w[k] = q0.w;
+        x[k] = q1.x; y[k] = q1.y; z[k] = q1.z;
+#pragma unroll
+        for (int i = 0; i < RL::NA; ++i) av[k][i] = i < g.vs_a ? at[i] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < RL::NP; ++i) pv[k][i] = i < g.vs_p ? (g.vs_a ? at[(3 + i) & 7] : at[i]) : 0.0f;
+      } else {
+        x[k] = vp[4]; y[k] = vp[5]; z[k] = vp[6]; w[k] = vp[3];
+        for (int i = 0; i < RL::NA; ++i) av[k][i] = i < g.vs_a ? vp[g.off_a + i] : 0.0f;
+        for (int i = 0; i < RL::NP; ++i) pv[k][i] = i < g.vs_p ? vp[g.off_p + i] : 0.0f;
+      }
     }
     float* rec = stage + threadIdx.x * RL::R;
     uint32_t tiles = 0;
@@ -595,17 +604,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
       if (RL::IZ) param_eq(z[0], z[1], z[2], e0, e1, e2, factor, eq + 3 * RL::EQ_Z);
       const float iw0 = swr_div(1.0f, w[0]), iw1 = swr_div(1.0f, w[1]), iw2 = swr_div(1.0f, w[2]);
       if (RL::IW) param_eq(iw0, iw1, iw2, e0, e1, e2, factor, eq + 3 * RL::EQ_W);
-      for (int i = 0; i < RL::NA; ++i) {
-        float a[3];
-        for (int k = 0; k < 3; ++k) a[k] = i < g.vs_a ? vp[k][g.off_a + i] : 0.0f;
-        param_eq(a[0], a[1], a[2], e0, e1, e2, factor, eq + 3 * (RL::EQ_A + i));
-      }
-      for (int i = 0; i < RL::NP; ++i) {
-        float a[3];
-        for (int k = 0; k < 3; ++k) a[k] = i < g.vs_p ? vp[k][g.off_p + i] : 0.0f;
-        param_eq(swr_mul(a[0], iw0), swr_mul(a[1], iw1), swr_mul(a[2], iw2), e0, e1, e2, factor,
+      for (int i = 0; i < RL::NA; ++i) param_eq(av[0][i], av[1][i], av[2][i], e0, e1, e2, factor, eq + 3 * (RL::EQ_A + i));
+      for (int i = 0; i < RL::NP; ++i)
+        param_eq(swr_mul(pv[0][i], iw0), swr_mul(pv[1][i], iw1), swr_mul(pv[2][i], iw2), e0, e1, e2, factor,
                  eq + 3 * (RL::EQ_P + i));
-      }
       // Raster mode (Rasterizer.h:414-446); Adaptive compares the float ratio as double.
       bool block = D.raster_mode == 1;
       if (D.raster_mode == 2) {

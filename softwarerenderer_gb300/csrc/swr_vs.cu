@@ -17,12 +17,12 @@ void run_vertex(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase
 
 template <class VS>
 void run_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_count<VS::AVarCount, VS::PVarCount><<<2 * nbatches, 256, 0, s>>>(a);
+  if (nbatches) k_assemble_count<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
 }
 
 template <class VS>
 void run_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<2 * nbatches, 256, 0, s>>>(a);
+  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
 }
 
 template <class VS>
