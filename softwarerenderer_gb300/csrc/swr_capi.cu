@@ -22,7 +22,7 @@ constexpr int kSingleSlots = 8;            // pinned descriptor slots of single 
 constexpr size_t kSingleSlotBytes = 1024;  // >= sizeof(SwrDrawDesc) + sizeof(SwrTargetDesc)
 constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CTA (bounds one warp's bitmap)
 constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
-constexpr int kStickyBase = 8;
+constexpr int kStickyBase = SWR_ST_STICKY;
 
 // Descriptor upload from pinned host staging (device-accessible under unified addressing)
 // by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
@@ -50,13 +50,7 @@ __global__ void k_stage_copy(const StageCopy sc) {
   }
 }
 
-__global__ void k_close_draw(uint32_t* st, uint32_t* big_count) {
-  for (int i = SWR_ST_CLIP_SLOTS; i <= SWR_ST_FRAGS; ++i) {
-    const uint32_t v = st[i];
-    if (v > st[kStickyBase + i]) st[kStickyBase + i] = v;
-  }
-  if (big_count) *big_count = 0u;  // the large-cell list of this draw's binning is consumed
-}
+__global__ void k_close_draw(uint32_t* st) { swr_close_status(st); }
 
 struct Buffer {
   void* p = nullptr;
@@ -205,7 +199,11 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->keys1.ensure((size_t)c->cap_pairs * 4 + 16);
   ok &= c->vals1.ensure((size_t)c->cap_pairs * 4 + 16);
   ok &= c->tile_start.ensure((size_t)(ntiles + 1) * 4 + 16);
-  ok &= c->cell_count.ensure((size_t)ntiles * SWR_SEGS * 4 + 16);
+  if (c->cell_count.bytes < (size_t)ntiles * SWR_SEGS * 4 + 16) {
+    // the per-cell counters start at zero and every draw leaves them at zero (k_fill_bins)
+    ok &= c->cell_count.ensure((size_t)ntiles * SWR_SEGS * 4 + 16);
+    ok &= c->cell_count.p && cudaMemset(c->cell_count.p, 0, c->cell_count.bytes) == cudaSuccess;
+  }
   ok &= c->cell_start.ensure(((size_t)ntiles * SWR_SEGS + 1) * 4 + 16);
   if (c->big_cells.bytes < ((size_t)ntiles * SWR_SEGS + 2) * 4) {
     ok &= c->big_cells.ensure(((size_t)ntiles * SWR_SEGS + 2) * 4 + 16);
@@ -258,7 +256,6 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   const uint32_t ncells = ntiles * SWR_SEGS;
   int seg_shift = 0;
   while (((uint64_t)(c->cap_prims > 0 ? c->cap_prims - 1 : 0) >> seg_shift) >= SWR_SEGS) ++seg_shift;
-  cudaMemsetAsync(c->cell_count.p, 0, (size_t)ncells * 4, s);
   SetupArgs sa;
   memset(&sa, 0, sizeof(sa));
   sa.tris = c->tris.as<uint4>();
@@ -291,8 +288,8 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // the segment's id range in shared memory, while that range fits in kBigSortSmem
   const size_t bm_bytes = ((size_t)1 << seg_shift) / 8;  // one warp's bitmap
   const int big_warps = (int)std::min<size_t>(8, std::max<size_t>(1, kBigSortSmem / std::max<size_t>(bm_bytes, 1)));
-  // (buffer: [list length, spare, cell ids...]; the length is zeroed when the buffer is
-  // allocated and reset by k_close_draw at the end of every draw)
+  // (buffer: [list length, blocks done, cell ids...]; both words are zeroed when the buffer
+  // is allocated and reset by k_sort_big's last block, which also closes the draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
   k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
@@ -323,8 +320,11 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.tile_counter = nullptr;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
-  k_close_draw<<<1, 1, 0, s>>>(st, big);
-  c->launches += 1 + 2 + 1 + 1 + (ntiles ? 1 : 0) + 1;
+  if (!use_big) {
+    k_close_draw<<<1, 1, 0, s>>>(st);
+    c->launches += 1;
+  }
+  c->launches += 1 + 2 + 1 + 1 + (ntiles ? 1 : 0);
   return cuda_err(cudaGetLastError());
 }
 
@@ -392,7 +392,7 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
   sh.status_w = st;
   ps->lp_shade(sh, s);
   mark(c, 5, s);
-  k_close_draw<<<1, 1, 0, s>>>(st, nullptr);
+  k_close_draw<<<1, 1, 0, s>>>(st);
   c->launches += 1 + 2 + 1 + 3 * ((bits + 7) / 8) + 1 + 1;
   return cuda_err(cudaGetLastError());
 }

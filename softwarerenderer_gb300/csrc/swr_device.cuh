@@ -45,6 +45,16 @@ enum SwrStatusFlags {
   SWR_F_BAD_GRAD_INPUT = 128,  // backward: a winner or source id beyond the given counts
 };
 #define SWR_F_ANY_OVERFLOW (SWR_F_CLIP_OVERFLOW | SWR_F_PRIM_OVERFLOW | SWR_F_PAIR_OVERFLOW | SWR_F_FRAG_OVERFLOW)
+#define SWR_ST_STICKY 8  // words SWR_ST_STICKY + i keep the largest value word i reached (i = CLIP_SLOTS..FRAGS)
+
+// End of a draw: the sticky maxima of the queue sizes it requested (the host grows its
+// queues from them after an overflow).  One thread, after every stage that counts.
+__device__ __forceinline__ void swr_close_status(uint32_t* st) {
+  for (int i = SWR_ST_CLIP_SLOTS; i <= SWR_ST_FRAGS; ++i) {
+    const uint32_t v = st[i];
+    if (v > st[SWR_ST_STICKY + i]) st[SWR_ST_STICKY + i] = v;
+  }
+}
 
 // One draw of a submission: the state VertexProcessor and Rasterizer hold for one
 // drawElements call (VertexProcessor.h:140-151, Rasterizer.h:54-63).

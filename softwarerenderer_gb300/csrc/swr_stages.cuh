@@ -799,13 +799,16 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
                                                    const SwrTargetDesc* targets, int tile, uint32_t* bin,
                                                    uint32_t* status_w) {
   typedef Rec<PS> RL;
-  if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  // cell_count is all zero between draws: every entry counted by k_setup is taken back
+  // here, and a draw that stops early zeroes the counts instead
   const uint32_t total = cell_start[ncells];
-  if (total > cap_pairs) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+  const bool overflow = status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW;
+  if (overflow || total > cap_pairs) {
+    if (!overflow && blockIdx.x == 0 && threadIdx.x == 0) {
       atomicOr(&status_w[SWR_ST_FLAGS], SWR_F_PAIR_OVERFLOW);
       status_w[SWR_ST_PAIRS] = total;
     }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += gridDim.x * blockDim.x) cell_count[i] = 0u;
     return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) status_w[SWR_ST_PAIRS] = total;
@@ -813,10 +816,12 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
   if (np > cap_prims) np = cap_prims;
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
     if (!tile_count[p]) continue;
-    const float* rec = recs + (size_t)p * RL::R;
-    const SwrTargetDesc& T = targets[draws[__float_as_int(rec[1])].target];
-    const int tx0 = __float_as_int(rec[2]) / tile, ty0 = __float_as_int(rec[3]) / tile;
-    const int tx1 = __float_as_int(rec[4]) / tile, ty1 = __float_as_int(rec[5]) / tile;
+    // record words 1-5: draw, pixel box (two float4 reads of the 16-byte aligned record)
+    const float4 q0 = __ldg((const float4*)(recs + (size_t)p * RL::R));
+    const float4 q1 = __ldg((const float4*)(recs + (size_t)p * RL::R) + 1);
+    const SwrTargetDesc& T = targets[draws[__float_as_int(q0.y)].target];
+    const int tx0 = __float_as_int(q0.z) / tile, ty0 = __float_as_int(q0.w) / tile;
+    const int tx1 = __float_as_int(q1.x) / tile, ty1 = __float_as_int(q1.y) / tile;
     const uint32_t seg = p >> seg_shift;
     for (int ty = ty0; ty <= ty1; ++ty)
       for (int tx = tx0; tx <= tx1; ++tx) {
@@ -894,9 +899,9 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
 // id (only the words between the cell's smallest and largest id are touched), prefix-count
 // the words across the lanes, write the set bits out in order.  Dynamic shared memory:
 // (1 << shift) / 8 bytes per warp.  big_count[0] is the list length (reset after the draw).
-static __global__ void k_sort_big(const uint32_t* status, const uint32_t* cell_start, uint32_t ncells,
+static __global__ void k_sort_big(uint32_t* status, const uint32_t* cell_start, uint32_t ncells,
                                   uint32_t cap_pairs, int seg_shift, const uint32_t* in, uint32_t* out,
-                                  const uint32_t* big_list, const uint32_t* big_count) {
+                                  const uint32_t* big_list, uint32_t* big_count) {
   extern __shared__ uint32_t smem_bm[];
   const bool skip = (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) || cell_start[ncells] > cap_pairs;
   const uint32_t nbig = skip ? 0u : min(*(volatile uint32_t*)big_count, ncells);
@@ -951,6 +956,17 @@ static __global__ void k_sort_big(const uint32_t* status, const uint32_t* cell_s
       }
     }
     __syncwarp();
+  }
+  // The last block to finish closes the draw: the list ([length, blocks done]) is consumed,
+  // and every counting stage has run (the tile raster counts only fragments).
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&big_count[1], 1u) == gridDim.x - 1) {
+      swr_close_status(status);
+      big_count[0] = 0u;
+      big_count[1] = 0u;
+    }
   }
 }
 
