@@ -1194,7 +1194,9 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   constexpr bool kCull = SWR_DEPTH_CULL && SwrDepthCull<PS>::value;
   __shared__ uint32_t swd[8];  // per warp: order key of the largest depth its pixels hold
   __shared__ float sdmax;      // over the tile (+inf: some pixel holds +inf, nothing can be culled)
-  __shared__ uint32_t sculled[2];  // chunk primitives whose fragments are only counted
+  constexpr int NW = CH / 32;      // 32-primitive words of a chunk
+  static_assert(CH % 32 == 0 && CH <= 128, "chunks of 32, 64, 96 or 128 primitives");
+  __shared__ uint32_t sculled[NW];  // chunk primitives whose fragments are only counted
   __shared__ int sminx[kCull ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1388,14 +1390,14 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       }
     }
     __syncthreads();
-    // C1 set-up (warps 0 and 1 measure primitives lane and lane + 32, warp 0 scans): compact
-    // the small primitives' fragments (a prefix of the chunk's small primitives whose
-    // fragments fit in FB).
+    // C1 set-up (one thread per primitive in warps 0..NW-1, warp 0 scans): compact the small
+    // primitives' fragments (a prefix of the chunk's small primitives whose fragments fit in
+    // FB).
     // Depth-tested shaders: a primitive whose z is provably not below the largest depth of
     // the tile's pixels at the chunk's start fails every depth test of the chunk (depths only
     // decrease), so its fragments are only counted (sculled).  A tile still holding a +inf
     // depth can cull nothing (z is finite), and skips the test.
-    if (warp < 2) {
+    if (warp < NW) {
       const float dmax = kCull ? sdmax : 0.0f;
       const bool try_cull = kCull && dmax < __int_as_float(0x7f800000);
       auto prim_info = [&](int k, uint32_t& cnt, bool& culled) {
@@ -1437,48 +1439,50 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
                                (float)(oy + cy0) + 0.5f, y1, X, y1, steps, dmax);
         }
       };
+      // warps 0..NW-1 measure primitives warp * 32 + lane; warp 0 scans all of them
       uint32_t cnt0;
       bool cul0;
       prim_info(threadIdx.x, cnt0, cul0);
-      if (warp == 1) {  // hand primitive lane + 32 to warp 0 through sex / scomp
+      if (warp > 0) {  // hand the primitive to warp 0 through sex / scomp
         sex[threadIdx.x] = cnt0;
         scomp[threadIdx.x] = cul0;
       }
-      asm volatile("bar.sync 1, 64;" ::: "memory");  // warps 0 and 1 only
+      if (NW > 1) asm volatile("bar.sync 1, %0;" ::"r"(CH) : "memory");  // warps 0..NW-1 only
       if (warp == 0) {
-        const uint32_t cnt1 = sex[lane + 32];
-        const bool cul1 = scomp[lane + 32] != 0;
-        const uint32_t cand0 = cnt0 <= SMALL && !cul0 ? cnt0 : 0u;
-        const uint32_t cand1 = cnt1 <= SMALL && !cul1 ? cnt1 : 0u;
-        uint32_t inc0 = cand0, inc1 = cand1;  // inclusive scans over lanes
+        uint32_t cnt[NW], cand[NW], inc[NW];
+        bool cul[NW];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y0 = __shfl_up_sync(0xffffffffu, inc0, o), y1 = __shfl_up_sync(0xffffffffu, inc1, o);
-          if (lane >= o) {
-            inc0 += y0;
-            inc1 += y1;
+        for (int w = 0; w < NW; ++w) {
+          cnt[w] = w ? sex[w * 32 + lane] : cnt0;
+          cul[w] = w ? scomp[w * 32 + lane] != 0 : cul0;
+          cand[w] = cnt[w] <= SMALL && !cul[w] ? cnt[w] : 0u;
+          inc[w] = cand[w];
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {  // inclusive scans over lanes
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc[w], o);
+            if (lane >= o) inc[w] += y;
           }
         }
-        const uint32_t ex0 = inc0 - cand0, ex1 = __shfl_sync(0xffffffffu, inc0, 31) + inc1 - cand1;
-        const bool comp0 = !cul0 && cnt0 <= SMALL && ex0 + cnt0 <= FB;
-        const bool comp1 = !cul1 && cnt1 <= SMALL && ex1 + cnt1 <= FB;
-        if (lane < n) {
-          sex[lane] = ex0;
-          scomp[lane] = comp0 ? 1 : 0;
+        uint32_t carry = 0, hi = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          const uint32_t ex = carry + inc[w] - cand[w];
+          carry += __shfl_sync(0xffffffffu, inc[w], 31);
+          const bool comp = !cul[w] && cnt[w] <= SMALL && ex + cnt[w] <= FB;
+          if (w * 32 + lane < n) {
+            sex[w * 32 + lane] = ex;
+            scomp[w * 32 + lane] = comp ? 1 : 0;
+          }
+          if (comp && cnt[w]) hi = max(hi, ex + cnt[w]);
+          if (kCull) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, cul[w]);
+            if (lane == 0) sculled[w] = bal;
+          }
         }
-        if (lane + 32 < n) {
-          sex[lane + 32] = ex1;
-          scomp[lane + 32] = comp1 ? 1 : 0;
-        }
-        const uint32_t hi = max(comp0 && cnt0 ? ex0 + cnt0 : 0u, comp1 && cnt1 ? ex1 + cnt1 : 0u);
         const uint32_t nc_max = __reduce_max_sync(0xffffffffu, hi);
-        if (kCull) {
-          const uint32_t b0 = __ballot_sync(0xffffffffu, cul0), b1 = __ballot_sync(0xffffffffu, cul1);
-          if (lane == 0) {
-            sculled[0] = b0;
-            sculled[1] = b1;
-          }
-        }
         if (lane == 0) snc = nc_max;
       }
     }
@@ -1536,24 +1540,32 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
       const int half = (py[q] >> 2) & 1;
-      uint64_t hits = 0;
-      for (int k0 = 0; k0 < n; k0 += 32) {
-        const int k = k0 + lane;
+      constexpr int HW = (CH + 63) / 64;  // 64-primitive words
+      uint64_t hw[HW];
+#pragma unroll
+      for (int w = 0; w < HW; ++w) hw[w] = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const int k = w * 32 + lane;
         const bool h = k < n && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
-        hits |= (uint64_t)__ballot_sync(0xffffffffu, h) << k0;
+        hw[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
       }
       const int bit = (py[q] & 7) * 8 + (px[q] & 7);
       if (kCull && sdmax < __int_as_float(0x7f800000)) {
         // culled primitives' fragments fail the depth test: they are only counted, in any
         // order (counters commute), outside the primitive-order walk
-        uint64_t ch = hits & ((uint64_t)sculled[0] | ((uint64_t)sculled[1] << 32));
-        hits &= ~ch;
-        while (ch) {
-          const int k = __ffsll((long long)ch) - 1;
-          ch &= ch - 1ull;
-          if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
-            frags++;
-            PS::earlyReject(__int_as_float(0x7f800000), st[q]);  // counts the rejected fragment
+#pragma unroll
+        for (int w = 0; w < HW; ++w) {
+          const uint64_t cm = (uint64_t)sculled[2 * w] | (2 * w + 1 < NW ? (uint64_t)sculled[2 * w + 1] << 32 : 0ull);
+          uint64_t ch = hw[w] & cm;
+          hw[w] &= ~ch;
+          while (ch) {
+            const int k = w * 64 + __ffsll((long long)ch) - 1;
+            ch &= ch - 1ull;
+            if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
+              frags++;
+              PS::earlyReject(__int_as_float(0x7f800000), st[q]);  // counts the rejected fragment
+            }
           }
         }
       }
@@ -1562,24 +1574,39 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         // only the chunk's last covering primitive shades; the others only count
         int last = -1;
         uint32_t cnt = 0;
-        while (hits) {
-          const int k = __ffsll((long long)hits) - 1;
-          hits &= hits - 1ull;
-          if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
-            ++cnt;
-            last = k;
+#pragma unroll
+        for (int w = 0; w < HW; ++w) {
+          uint64_t h = hw[w];
+          while (h) {
+            const int k = w * 64 + __ffsll((long long)h) - 1;
+            h &= h - 1ull;
+            if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
+              ++cnt;
+              last = k;
+            }
           }
         }
         if (cnt) {
-          hits = 1ull << last;
+#pragma unroll
+          for (int w = 0; w < HW; ++w) hw[w] = (last >> 6) == w ? 1ull << (last & 63) : 0ull;
           extra = cnt - 1;
           frags += extra;
           st[q].frags += extra;
           st[q].writes += extra;
         }
       }
-      while (hits) {
-        const int k = __ffsll((long long)hits) - 1;
+      // primitive-order walk over the words (one copy of the loop body)
+      uint64_t hits = hw[0];
+      uint64_t later = HW > 1 ? hw[HW - 1] : 0ull;
+      int kbase = 0;
+      while (true) {
+        if (!hits) {
+          if (HW == 1 || !later) break;
+          hits = later;
+          later = 0;
+          kbase = 64;
+        }
+        const int k = kbase + __ffsll((long long)hits) - 1;
         hits &= hits - 1ull;
         const uint64_t* mk = smask + k * NB;
         const uint64_t m = mk[blk[q]];
