@@ -241,7 +241,7 @@ struct PsTexNearest {
 // Lambert-lit procedural checker, depth-tested (config: dense icosphere).
 // AVar = normal, PVar = uv.
 struct PsLambert {
-  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5,
+  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 6,
          DepthCull = 0 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
@@ -280,7 +280,7 @@ struct PsLambert {
 
 // Lambert-lit and textured (nearest RGBA8), depth-tested (config: batched meshes).
 struct PsLambertTex {
-  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5,
+  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 6,
          DepthCull = 0 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
@@ -673,8 +673,9 @@ struct SwrOverwrite<PS, decltype((void)PS::Overwrite)> {
 // may therefore count, without interpolating, every fragment of a primitive whose z is
 // provably not below the largest depth held by the pixels it covers.  A shader may opt out
 // with DepthCull = 0.  The Lambert and differentiable shaders do: their tile rasters run at
-// 5 CTAs per SM in 48 registers, where the cull's code made the Lambert rasters 3-5 % slower
-// on their single-mesh workloads (which have nothing to cull) and the differentiable one spill.
+// 5-6 CTAs per SM in 40-48 registers, where the cull's code made the Lambert rasters 3-5 %
+// slower on their single-mesh workloads (which have nothing to cull) and the differentiable
+// one spill.
 template <class PS, class = void>
 struct SwrDepthCull {
   enum { value = PS::HasDepth && PS::InterpolateZ && !SwrOverwrite<PS>::value };

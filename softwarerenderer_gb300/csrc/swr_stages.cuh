@@ -1155,8 +1155,9 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 //      Block-mode blocks (the reference's corner test) and builds Span-mode rows from
 //      [xl, xr) (kept as each row's interpolation start); partially covered blocks are then
 //      finished by 8 lanes each, one row per lane, with the reference's stepped edge tests;
-//   C0. depth-tested shaders: primitives whose z cannot pass any depth test of the chunk
-//      (z_not_below against the tile's largest depth) are only counted;
+//   C0. depth-tested shaders: per 8 x 4 pixel region, primitives whose z cannot pass any
+//      depth test of the chunk there (z_not_below against the region's largest depth) are
+//      only counted;
 //   C1. small primitives (<= 64 covered pixels in the tile, up to FB fragments per chunk)
 //      are compacted: one thread per covered fragment rebuilds the stepped interpolants and
 //      evaluates the pixel shader's pure shade() at full SIMT width;
@@ -1192,11 +1193,13 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   static_assert(sizeof(srec4) >= SWR_RASTER_SORT * 4, "raw bin staging fits the record area");
   __shared__ uint32_t stile;
   constexpr bool kCull = SWR_DEPTH_CULL && SwrDepthCull<PS>::value;
-  __shared__ uint32_t swd[8];  // per warp: order key of the largest depth its pixels hold
-  __shared__ float sdmax;      // over the tile (+inf: some pixel holds +inf, nothing can be culled)
+  // Depth cull regions: the 8 x 4 pixels of one warp in one sub-tile (region q * 8 + warp).
+  constexpr int NREG = 8 * PPT;
+  __shared__ uint32_t swd[NREG];  // per region: order key of the largest depth it holds
+  __shared__ uint32_t scull_on;   // some region holds no +inf depth (0: nothing can be culled)
   constexpr int NW = CH / 32;      // 32-primitive words of a chunk
   static_assert(CH % 32 == 0 && CH <= 128, "chunks of 32, 64, 96 or 128 primitives");
-  __shared__ uint32_t sculled[NW];  // chunk primitives whose fragments are only counted
+  __shared__ uint32_t sculr[kCull ? NREG * NW : 1];  // per region: primitives only counted there
   __shared__ int sminx[kCull ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1271,28 +1274,26 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snpart = 0;
     if (kCull && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
-    // Tile depth bound at the chunk's start (depth-tested shaders, tiles of more than one
-    // chunk).  A tile with a pixel still at +inf can cull nothing (z is finite), which the
-    // barrier's OR tells for free; otherwise the largest of the warps' order-preserving keys
-    // of their largest depths (NaN depths, which every fragment fails, and pixels outside
-    // the target are ignored).
-    int tile_inf = 1;
+    // Region depth bounds at the chunk's start (depth-tested shaders, tiles of more than one
+    // chunk): per region an order-preserving key of the largest depth its pixels hold (NaN
+    // depths, which every fragment fails, and pixels outside the target are ignored; key 0:
+    // none usable).  A region holding +inf can cull nothing (z is finite); the barrier's OR
+    // tells whether any region can.
+    int any_ok = 0;
     bool cull_tile = false;
-    bool my_inf = false;
+    bool my_ok = false;
     if constexpr (kCull) {
       cull_tile = e - b > (uint32_t)CH;
       if (cull_tile) {
-        uint32_t key = 0;
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
           const float dq = swr_state_depth(st[q]);
           const uint32_t u = __float_as_uint(dq);
           const uint32_t kq = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-          my_inf |= in[q] && dq == __int_as_float(0x7f800000);
-          if (in[q] && !swr_isnan(dq)) key = max(key, kq);
+          const uint32_t key = __reduce_max_sync(0xffffffffu, in[q] && !swr_isnan(dq) ? kq : 0u);
+          if (lane == 0) swd[q * 8 + warp] = key;
+          my_ok |= key != 0u && key < 0xff800000u;  // uniform per warp
         }
-        key = __reduce_max_sync(0xffffffffu, key);
-        if (lane == 0) swd[warp] = key;
       }
     }
     // A: the chunk's setup records (ids read from the bin directly: sids is published by
@@ -1308,22 +1309,12 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       }
     }
     if (cull_tile)
-      tile_inf = __syncthreads_or(my_inf);
+      any_ok = __syncthreads_or(my_ok);
     else
       __syncthreads();
     // B1: coverage per (primitive, block).  Fully covered / skipped blocks and Span rows are
     // finished here; partially covered Block-mode blocks are queued for B2.
-    if (kCull && threadIdx.x == 0) {
-      float d = __int_as_float(0x7f800000);
-      if (!tile_inf) {
-        uint32_t key = swd[0];
-#pragma unroll
-        for (int w = 1; w < 8; ++w) key = max(key, swd[w]);
-        // key 0: no pixel with a usable depth -> NaN, which culls nothing
-        d = __uint_as_float((key & 0x80000000u) ? (key & 0x7fffffffu) : ~key);
-      }
-      sdmax = d;
-    }
+    if (kCull && threadIdx.x == 0) scull_on = any_ok;
     for (int i = threadIdx.x; i < n * NB; i += 256) {
       const int k = i / NB, j = i - k * NB;
       const float* r = srec + k * RL::R;
@@ -1390,53 +1381,76 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       }
     }
     __syncthreads();
+    // C0 (depth-tested shaders): per (region, primitive) whether every covered pixel's z is
+    // provably not below the region's largest depth at the chunk's start (z_not_below over
+    // the covered pixels' box in the region).  Depths only decrease, so such fragments fail
+    // their depth tests: the primitive is only counted there.
+    if (kCull && scull_on) {
+      for (int t = threadIdx.x; t < NREG * CH; t += 256) {
+        const int reg = t / CH, k = t - reg * CH;  // reg uniform per warp (CH is a multiple of 32)
+        bool culled = false;
+        if (k < n && (__float_as_int(srec[k * RL::R]) & 1)) {
+          const int q = reg >> 3, w = reg & 7, hb = w >> 1;
+          const int lx0 = (q % (TILE / 16)) * 16 + (hb & 1) * 8;
+          const int ly0 = (q / (TILE / 16)) * 16 + (hb >> 1) * 8 + (w & 1) * 4;
+          const uint32_t mh = (uint32_t)(smask[k * NB + (ly0 >> 3) * NBX + (lx0 >> 3)] >> ((w & 1) * 32));
+          const uint32_t key = swd[reg];
+          if (mh && key != 0u && key < 0xff800000u) {
+            const float dmax = __uint_as_float((key & 0x80000000u) ? (key & 0x7fffffffu) : ~key);
+            uint32_t c = mh | (mh >> 16);
+            c |= c >> 8;
+            c &= 0xffu;
+            const int x0 = ox + lx0 + __ffs(c) - 1, x1 = ox + lx0 + 31 - __clz(c);
+            const int y0 = oy + ly0 + ((__ffs(mh) - 1) >> 3), y1 = oy + ly0 + ((31 - __clz(mh)) >> 3);
+            const float* r = srec + k * RL::R;
+            // walk bounds: Block mode steps <= 7 rows then <= 7 columns inside the block;
+            // Span mode steps from the row's span start (every covered pixel lies in a row
+            // whose span reaches the tile) to the pixel
+            int steps = 2 * (SWR_BLOCK - 1);
+            float X = (float)x1 + 0.5f;
+            if (!(__float_as_int(r[0]) & 2)) {
+              const int smin = sminx[k];
+              steps = max(0, x1 - smin);
+              if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
+            }
+            const float* zq = r + RL::EQ0 + 3 * RL::EQ_Z;
+            const float fy1 = (float)y1 + 0.5f;
+            culled = z_not_below(zq[0], zq[1], zq[2], (float)x0 + 0.5f, (float)x1 + 0.5f, (float)y0 + 0.5f, fy1, X,
+                                 fy1, steps, dmax);
+          }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, culled);
+        if (lane == 0) sculr[reg * NW + (k >> 5)] = bal;
+      }
+      __syncthreads();
+    }
     // C1 set-up (one thread per primitive in warps 0..NW-1, warp 0 scans): compact the small
     // primitives' fragments (a prefix of the chunk's small primitives whose fragments fit in
-    // FB).
-    // Depth-tested shaders: a primitive whose z is provably not below the largest depth of
-    // the tile's pixels at the chunk's start fails every depth test of the chunk (depths only
-    // decrease), so its fragments are only counted (sculled).  A tile still holding a +inf
-    // depth can cull nothing (z is finite), and skips the test.
+    // FB), leaving out primitives culled in every region they cover.
     if (warp < NW) {
-      const float dmax = kCull ? sdmax : 0.0f;
-      const bool try_cull = kCull && dmax < __int_as_float(0x7f800000);
+      const bool try_cull = kCull && scull_on;
+      // cnt: the primitive's covered pixels in the tile; culled: culled in every region it
+      // covers (its fragments are then left out of the compaction)
       auto prim_info = [&](int k, uint32_t& cnt, bool& culled) {
         cnt = 0;
         culled = false;
         if (k >= n) return;
         const float* r = srec + k * RL::R;
         if (!(__float_as_int(r[0]) & 1)) return;
-        int cx0 = TILE, cx1 = -1, cy0 = TILE, cy1 = -1;  // covered pixels' box in the tile
         for (int j = 0; j < NB; ++j) {
           const uint64_t m = smask[k * NB + j];
           cnt += __popc((uint32_t)m) + __popc((uint32_t)(m >> 32));
-          if (kCull && try_cull && m) {
-            uint32_t cols = (uint32_t)m | (uint32_t)(m >> 32);
-            cols |= cols >> 16;
-            cols |= cols >> 8;
-            cols &= 0xffu;
-            const int bx = (j % NBX) * SWR_BLOCK, by = (j / NBX) * SWR_BLOCK;
-            cx0 = min(cx0, bx + __ffs(cols) - 1);
-            cx1 = max(cx1, bx + 31 - __clz(cols));
-            cy0 = min(cy0, by + ((__ffsll((long long)m) - 1) >> 3));
-            cy1 = max(cy1, by + ((63 - __clzll((long long)m)) >> 3));
-          }
         }
         if (kCull && try_cull && cnt) {
-          // walk bounds: Block mode steps <= 7 rows then <= 7 columns inside the block;
-          // Span mode steps from the row's span start to the pixel
-          int steps = 2 * (SWR_BLOCK - 1);
-          float X = (float)(ox + cx1) + 0.5f;
-          if (!(__float_as_int(r[0]) & 2)) {
-            // every covered pixel lies in a row whose span reaches the tile
-            const int smin = sminx[k];
-            steps = max(0, ox + cx1 - smin);
-            if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
+          bool all = true;
+          for (int reg = 0; reg < NREG; ++reg) {
+            const int q = reg >> 3, w = reg & 7, hb = w >> 1;
+            const int lx0 = (q % (TILE / 16)) * 16 + (hb & 1) * 8;
+            const int ly0 = (q / (TILE / 16)) * 16 + (hb >> 1) * 8 + (w & 1) * 4;
+            const uint32_t mh = (uint32_t)(smask[k * NB + (ly0 >> 3) * NBX + (lx0 >> 3)] >> ((w & 1) * 32));
+            if (mh && !((sculr[reg * NW + (k >> 5)] >> (k & 31)) & 1u)) all = false;
           }
-          const float* zq = r + RL::EQ0 + 3 * RL::EQ_Z;
-          const float y1 = (float)(oy + cy1) + 0.5f;
-          culled = z_not_below(zq[0], zq[1], zq[2], (float)(ox + cx0) + 0.5f, (float)(ox + cx1) + 0.5f,
-                               (float)(oy + cy0) + 0.5f, y1, X, y1, steps, dmax);
+          culled = all;
         }
       };
       // warps 0..NW-1 measure primitives warp * 32 + lane; warp 0 scans all of them
@@ -1477,10 +1491,6 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             scomp[w * 32 + lane] = comp ? 1 : 0;
           }
           if (comp && cnt[w]) hi = max(hi, ex + cnt[w]);
-          if (kCull) {
-            const uint32_t bal = __ballot_sync(0xffffffffu, cul[w]);
-            if (lane == 0) sculled[w] = bal;
-          }
         }
         const uint32_t nc_max = __reduce_max_sync(0xffffffffu, hi);
         if (lane == 0) snc = nc_max;
@@ -1551,12 +1561,13 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         hw[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
       }
       const int bit = (py[q] & 7) * 8 + (px[q] & 7);
-      if (kCull && sdmax < __int_as_float(0x7f800000)) {
-        // culled primitives' fragments fail the depth test: they are only counted, in any
-        // order (counters commute), outside the primitive-order walk
+      if (kCull && scull_on) {
+        // primitives culled in this warp's region: their fragments fail the depth test and
+        // are only counted, in any order (counters commute), outside the primitive-order walk
+        const uint32_t* cr = sculr + (q * 8 + warp) * NW;
 #pragma unroll
         for (int w = 0; w < HW; ++w) {
-          const uint64_t cm = (uint64_t)sculled[2 * w] | (2 * w + 1 < NW ? (uint64_t)sculled[2 * w + 1] << 32 : 0ull);
+          const uint64_t cm = (uint64_t)cr[2 * w] | (2 * w + 1 < NW ? (uint64_t)cr[2 * w + 1] << 32 : 0ull);
           uint64_t ch = hw[w] & cm;
           hw[w] &= ~ch;
           while (ch) {
