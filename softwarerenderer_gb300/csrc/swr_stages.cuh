@@ -294,15 +294,9 @@ __device__ void assemble_one(const AssembleArgs& g, const SwrDrawDesc& D, uint32
   ex_kept = __popc(keep >> 1);
 }
 
-// Triangles [p0, p0 + count) of a draw (clamped to the draw): their 3 indices each are
-// loaded cooperatively (coalesced) into shared memory.  Returns the clamped count.
-__device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uint32_t p0, uint32_t* sidx,
-                                                       uint32_t count = SWR_BATCH_PRIMS) {
-  const uint32_t n = p0 < D.nprims ? min(count, D.nprims - p0) : 0u;
-  const uint32_t* src = D.indices + (size_t)3 * p0;
-  for (uint32_t i = threadIdx.x; i < 3 * n; i += blockDim.x) sidx[i] = src[i];
-  __syncthreads();
-  return n;
+// Triangles [p0, p0 + count) of a draw, clamped to the draw: their count.
+__device__ __forceinline__ uint32_t batch_count(const SwrDrawDesc& D, uint32_t p0, uint32_t count) {
+  return p0 < D.nprims ? min(count, D.nprims - p0) : 0u;
 }
 
 #define SWR_HALF (SWR_BATCH_PRIMS / 2)  // triangles per assembly CTA (half a batch)
@@ -312,15 +306,17 @@ __device__ __forceinline__ uint32_t load_batch_indices(const SwrDrawDesc& D, uin
 template <int A, int P>
 __global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
   __shared__ uint32_t tmp[64];
-  __shared__ uint32_t sidx[3 * SWR_HALF];
   const uint32_t hb = blockIdx.x, b = hb >> 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + (hb & 1) * SWR_HALF;
-  const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
+  const uint32_t n = batch_count(D, p0, SWR_HALF);
   uint32_t ik = 0, ek = 0;
   const uint32_t q = threadIdx.x;
-  if (q < n) assemble_one<A, P>(g, D, p0 + q, sidx[3 * q], sidx[3 * q + 1], sidx[3 * q + 2], ik, ek);
+  if (q < n) {
+    const uint32_t* ix = D.indices + (size_t)3 * (p0 + q);
+    assemble_one<A, P>(g, D, p0 + q, __ldg(ix), __ldg(ix + 1), __ldg(ix + 2), ik, ek);
+  }
   uint32_t tin, tex;
   swr_block_sum2(ik, ek, tmp, tin, tex);
   if (threadIdx.x == 0) g.batch_counts[hb] = make_uint2(tin, tex);
@@ -352,13 +348,12 @@ template <int A, int P>
 __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
   __shared__ uint32_t tmp[64];
   __shared__ uint32_t tmps[32];
-  __shared__ uint32_t sidx[3 * SWR_HALF];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t hb = blockIdx.x, b = hb >> 1, half = hb & 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + half * SWR_HALF;
-  const uint32_t n = load_batch_indices(D, p0, sidx, SWR_HALF);
+  const uint32_t n = batch_count(D, p0, SWR_HALF);
   uint32_t before = 0, dbefore = 0;
   for (uint32_t i = threadIdx.x; i < 2 * b; i += blockDim.x) {
     const uint32_t c = g.batch_counts[i].x + g.batch_counts[i].y;
@@ -377,8 +372,12 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
   const uint32_t in_base = base + (half ? c0.x : 0u);
   const uint32_t ex_base = base + batch_in + (half ? c0.y : 0u);
   const uint32_t q = threadIdx.x;
-  uint32_t fl = 0, slot = 0xffffffffu, keep = 0;
+  uint32_t fl = 0, slot = 0xffffffffu, keep = 0, i0 = 0, i1 = 0, i2 = 0;
   if (q < n) {
+    const uint32_t* ix = D.indices + (size_t)3 * (p0 + q);  // read early: used after the scan
+    i0 = __ldg(ix);
+    i1 = __ldg(ix + 1);
+    i2 = __ldg(ix + 2);
     fl = g.tri_flags[D.pbase + p0 + q];
     if (fl & 4) {
       slot = g.clip_slot[D.pbase + p0 + q];
@@ -410,7 +409,7 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
   };
   if (keep) {
     if (!(fl & 4)) {
-      uint32_t r0 = D.vbase + sidx[3 * q], r1 = D.vbase + sidx[3 * q + 1], r2 = D.vbase + sidx[3 * q + 2];
+      uint32_t r0 = D.vbase + i0, r1 = D.vbase + i1, r2 = D.vbase + i2;
       if (fl & 2) { const uint32_t t = r0; r0 = r2; r2 = t; }
       record_src(rin, p0 + q);
       g.tris[rin++] = make_uint4(r0, r1, r2, (uint32_t)d);
@@ -814,18 +813,31 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
   if (blockIdx.x == 0 && threadIdx.x == 0) status_w[SWR_ST_PAIRS] = total;
   uint32_t np = status[SWR_ST_PRIMS];
   if (np > cap_prims) np = cap_prims;
+  // draw 0's target, read up front: every primitive of a single-draw submission uses it
+  const SwrTargetDesc& T0 = targets[draws[0].target];
+  const uint32_t tb0 = T0.tile_base;
+  const int tw0 = T0.tiles_x;
+  const int tshift = __ffs(tile) - 1;  // tiles are 16 or 32 pixels; pixel boxes are >= 0
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-    if (!tile_count[p]) continue;
-    // record words 1-5: draw, pixel box (two float4 reads of the 16-byte aligned record)
+    // record words 0-5: flags (0: no tile, as tile_count), draw, pixel box (two float4
+    // reads of the 16-byte aligned record)
     const float4 q0 = __ldg((const float4*)(recs + (size_t)p * RL::R));
     const float4 q1 = __ldg((const float4*)(recs + (size_t)p * RL::R) + 1);
-    const SwrTargetDesc& T = targets[draws[__float_as_int(q0.y)].target];
-    const int tx0 = __float_as_int(q0.z) / tile, ty0 = __float_as_int(q0.w) / tile;
-    const int tx1 = __float_as_int(q1.x) / tile, ty1 = __float_as_int(q1.y) / tile;
+    if (!__float_as_int(q0.x)) continue;
+    const int d = __float_as_int(q0.y);
+    uint32_t tbase = tb0;
+    int tiles_x = tw0;
+    if (d != 0) {
+      const SwrTargetDesc& T = targets[draws[d].target];
+      tbase = T.tile_base;
+      tiles_x = T.tiles_x;
+    }
+    const int tx0 = __float_as_int(q0.z) >> tshift, ty0 = __float_as_int(q0.w) >> tshift;
+    const int tx1 = __float_as_int(q1.x) >> tshift, ty1 = __float_as_int(q1.y) >> tshift;
     const uint32_t seg = p >> seg_shift;
     for (int ty = ty0; ty <= ty1; ++ty)
       for (int tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t cell = (T.tile_base + (uint32_t)(ty * T.tiles_x + tx)) * SWR_SEGS + seg;
+        const uint32_t cell = (tbase + (uint32_t)(ty * tiles_x + tx)) * SWR_SEGS + seg;
         const uint32_t pos = atomicSub(&cell_count[cell], 1u) - 1u;
         bin[cell_start[cell] + pos] = p;
       }
