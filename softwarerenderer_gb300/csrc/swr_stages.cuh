@@ -1475,13 +1475,17 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       }
       if (NW > 1) asm volatile("bar.sync 1, %0;" ::"r"(CH) : "memory");  // warps 0..NW-1 only
       if (warp == 0) {
+        // Behind depths already written (a cull tile past its first chunk) most fragments fail
+        // their depth test: shading them ahead of the test (compaction) would be wasted, the
+        // in-place path tests z first.
+        const bool deep = kCull && scull_on;
         uint32_t cnt[NW], cand[NW], inc[NW];
         bool cul[NW];
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
           cnt[w] = w ? sex[w * 32 + lane] : cnt0;
           cul[w] = w ? scomp[w * 32 + lane] != 0 : cul0;
-          cand[w] = cnt[w] <= SMALL && !cul[w] ? cnt[w] : 0u;
+          cand[w] = cnt[w] <= SMALL && !cul[w] && !deep ? cnt[w] : 0u;
           inc[w] = cand[w];
         }
 #pragma unroll
@@ -1497,7 +1501,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         for (int w = 0; w < NW; ++w) {
           const uint32_t ex = carry + inc[w] - cand[w];
           carry += __shfl_sync(0xffffffffu, inc[w], 31);
-          const bool comp = !cul[w] && cnt[w] <= SMALL && ex + cnt[w] <= FB;
+          const bool comp = !cul[w] && !deep && cnt[w] <= SMALL && ex + cnt[w] <= FB;
           if (w * 32 + lane < n) {
             sex[w * 32 + lane] = ex;
             scomp[w * 32 + lane] = comp ? 1 : 0;
