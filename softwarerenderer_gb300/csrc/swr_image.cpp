@@ -16,17 +16,20 @@
 
 namespace {
 
-uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
-  static uint32_t table[256];
-  static bool init = false;
-  if (!init) {
+struct Crc32Table {
+  uint32_t t[256];
+  Crc32Table() {
     for (uint32_t i = 0; i < 256; ++i) {
       uint32_t c = i;
       for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xedb88320u ^ (c >> 1) : c >> 1;
-      table[i] = c;
+      t[i] = c;
     }
-    init = true;
   }
+};
+
+uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
+  static const Crc32Table tab;  // initialised once, thread-safe (C++11 function-local static)
+  const uint32_t* table = tab.t;
   crc = ~crc;
   for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
   return ~crc;
