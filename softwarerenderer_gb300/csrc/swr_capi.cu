@@ -251,7 +251,7 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
 // offsets, k_fill_bins scatters primitive ids into their cells, k_sort_cells restores the
 // primitive order inside each cell; a tile's bin is then its cells' contiguous range.
 int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int vs_a, int vs_p,
-                 uint32_t ntiles, cudaStream_t s, int ntargets = 1) {
+                 uint32_t ntiles, cudaStream_t s, int ntargets, bool has_span) {
   uint32_t* st = c->status.as<uint32_t>();
   const uint32_t ncells = ntiles * SWR_SEGS;
   int seg_shift = 0;
@@ -318,6 +318,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // one CTA per tile: a persistent grid pulling tiles from a counter measured no faster on
   // the dense mesh and slower where few tiles carry the work (they gather on fewer SMs)
   ra.tile_counter = nullptr;
+  ra.has_span = has_span ? 1 : 0;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);
   if (!use_big) {
@@ -646,7 +647,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   mark(c, 2, s);
   c->last_ntiles = ntiles;
   if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, T, s);
-  return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s);
+  return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s, 1, c->raster_mode != SWR_RASTER_BLOCK);
 }
 
 int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nverts, const int32_t* indices,
@@ -689,7 +690,7 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   mark(c, 2, s);
   c->last_ntiles = ntiles;
   if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, T, s);
-  return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s);
+  return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s, 1, c->raster_mode != SWR_RASTER_BLOCK);
 }
 
 int swr_set_graph_mode(swr_context* c, int on) {
@@ -705,6 +706,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   if (!vs || !ps) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   std::vector<SwrDrawDesc> D(n);
+  bool any_span = false;  // some item rasterizes in Span or Adaptive mode
   std::vector<SwrTargetDesc> T;
   std::vector<const void*> tcolor;
   std::vector<uint32_t> vbase(n), bbase(n), tbase;
@@ -765,6 +767,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     d.draw_mode = SWR_DRAW_TRIANGLE;
     d.cull = it.cull_mode;
     d.raster_mode = it.raster_mode;
+    any_span |= it.raster_mode != SWR_RASTER_BLOCK;
     d.vp_px = (float)it.viewport[2] / 2.0f;
     d.vp_py = (float)it.viewport[3] / 2.0f;
     d.vp_ox = (float)it.viewport[0] + d.vp_px;
@@ -893,7 +896,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   mark(c, 2, s);
   c->launches += (V ? 1 : 0) + (B ? 2 : 0);
   if (!q) q = cuda_err(cudaGetLastError());
-  rc = raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, (uint32_t)NT, s, ntg);
+  rc = raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, (uint32_t)NT, s, ntg, any_span);
   if (q) rc = q;
   c->use_draw_pbase = false;
   if (c->graph_mode) {

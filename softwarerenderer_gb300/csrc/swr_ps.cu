@@ -49,8 +49,14 @@ void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) 
       nsm = 152;
   }
   const uint32_t grid = a.tile_counter ? (ntiles < (uint32_t)nsm * 4u ? ntiles : (uint32_t)nsm * 4u) : ntiles;
-  if (tile == 32) k_raster<PS, 32, kChunk><<<grid, 256, 0, s>>>(a);
-  else k_raster<PS, 16, kChunk><<<grid, 256, 0, s>>>(a);
+  // Block-only submissions run the instantiation without the Span-mode passes
+  if (tile == 32) {
+    if (a.has_span) k_raster<PS, 32, kChunk, true><<<grid, 256, 0, s>>>(a);
+    else k_raster<PS, 32, kChunk, false><<<grid, 256, 0, s>>>(a);
+  } else {
+    if (a.has_span) k_raster<PS, 16, kChunk, true><<<grid, 256, 0, s>>>(a);
+    else k_raster<PS, 16, kChunk, false><<<grid, 256, 0, s>>>(a);
+  }
 }
 
 template <class PS>

@@ -1023,6 +1023,7 @@ struct RasterArgs {
   uint32_t* status_w;
   uint32_t ntiles;
   uint32_t* tile_counter;            // optional: persistent grid's next-tile counter (starts at 0)
+  int has_span;                      // some draw rasterizes in Span or Adaptive mode (selects k_raster<..., true>)
 };
 
 // v <- fl(v + a) repeated k times for 0 <= k <= 7 (steps inside one 8x8 block), as
@@ -1177,7 +1178,7 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 //      every covering fragment to the pixel's register-resident State: compacted fragments
 //      through apply(), others by rebuilding the interpolants in place (z first: a failing
 //      depth test needs nothing else) and drawPixel().
-template <class PS, int TILE, int CH>
+template <class PS, int TILE, int CH, bool SPAN>
 __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRasterOccupancy<PS>::value)
     k_raster(RasterArgs g) {
   typedef Rec<PS> RL;
@@ -1190,7 +1191,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   __shared__ float4 srec4[CH * RL::R / 4];
   float* srec = (float*)srec4;
   __shared__ uint64_t smask[CH * NB];
-  __shared__ int2 sspan[CH * TILE];
+  __shared__ int2 sspan[SPAN ? CH * TILE : 1];  // Span mode: each tile row's [xl, xr)
   __shared__ uint32_t sids[CH];
   __shared__ uint32_t sex[CH];   // compacted-fragment base (monotone over the chunk)
   __shared__ uint8_t scomp[CH];  // 1: compacted
@@ -1212,7 +1213,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   constexpr int NW = CH / 32;      // 32-primitive words of a chunk
   static_assert(CH % 32 == 0 && CH <= 128, "chunks of 32, 64, 96 or 128 primitives");
   __shared__ uint32_t sculr[kCull ? NREG * NW : 1];  // per region: primitives only counted there
-  __shared__ int sminx[kCull ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
+  __shared__ int sminx[kCull && SPAN ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
@@ -1285,7 +1286,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     __syncthreads();  // the previous chunk's shared state is no longer read; ssorted is complete
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snpart = 0;
-    if (kCull && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
+    if (kCull && SPAN && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
     // Region depth bounds at the chunk's start (depth-tested shaders, tiles of more than one
     // chunk): per region an order-preserving key of the largest depth its pixels hold (NaN
     // depths, which every fragment fails, and pixels outside the target are ignored; key 0:
@@ -1331,46 +1332,76 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       const int k = i / NB, j = i - k * NB;
       const float* r = srec + k * RL::R;
       const int flags = __float_as_int(r[0]);
+      if (SPAN && (flags & 3) == 1) continue;  // Span mode: rows below, masks after the barrier
       const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
       uint64_t m = 0;
       const bool hit = (flags & 1) && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
                        by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]);
-      if (flags & 2) {
-        if (hit) {
-          const int cls = block_class(r, flags, bx, by);
-          if (cls == 1) m = ~0ull;
-          if (cls == 2) spart[atomicAdd(&snpart, 1u)] = (uint16_t)i;
-        }
-      } else if (flags & 1) {
-        const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
-        int lmin = 0x7fffffff;
-        for (int rr = 0; rr < SWR_BLOCK; ++rr) {
-          const int y = by + rr;
-          // the row's span does not depend on this block's x-overlap: the column-0 task
-          // stores it for every block of the row
-          int2 sp = make_int2(1, 0);
-          if (y >= __float_as_int(r[3]) && y <= __float_as_int(r[5])) {
-            SpanHalf h;
-            bool any = true;
-            if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
-              h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
-            } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
-              h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
-            } else {
-              any = false;
-            }
-            if (any) span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
-          }
-          if ((j % NBX) == 0) sspan[k * TILE + (y - oy)] = sp;
-          if (kCull && sp.x < sp.y && sp.y > ox) lmin = min(lmin, sp.x);
-          const int c0b = max(sp.x, bx) - bx, c1b = min(sp.y, bx + SWR_BLOCK) - bx;
-          if (hit && c1b > c0b) m |= (((1ull << (c1b - c0b)) - 1ull) << c0b) << (rr * 8);
-        }
-        if (kCull && (j % NBX) == 0 && lmin != 0x7fffffff) atomicMin(&sminx[k], lmin);
+      if (hit) {  // Block mode (every valid primitive of a k_raster<..., false> launch)
+        const int cls = block_class(r, flags, bx, by);
+        if (cls == 1) m = ~0ull;
+        if (cls == 2) spart[atomicAdd(&snpart, 1u)] = (uint16_t)i;
       }
       smask[i] = m;
     }
-    __syncthreads();
+    if constexpr (SPAN) {
+      // B1 (Span mode): each tile row's span [xl, xr) of every primitive, once per row (kept
+      // as the row's interpolation start); the rows of one primitive are consecutive lanes,
+      // and whole warps iterate (the row reduction below shuffles across the warp)
+      for (int i = threadIdx.x; i < (n * TILE + 31) / 32 * 32; i += 256) {
+        const int k = i / TILE, row = i - k * TILE;
+        const float* r = srec + k * RL::R;
+        const int flags = k < n ? __float_as_int(r[0]) : 0;
+        int2 sp = make_int2(1, 0);
+        const int y = oy + row;
+        if ((flags & 3) == 1 && y >= __float_as_int(r[3]) && y <= __float_as_int(r[5])) {
+          SpanHalf h;
+          bool any = true;
+          if ((flags & 32) && y >= __float_as_int(r[6]) && y < __float_as_int(r[7])) {
+            h.ox = r[8]; h.oy = r[9]; h.is1 = r[10]; h.is2 = r[11];
+          } else if ((flags & 64) && y > __float_as_int(r[13]) && y <= __float_as_int(r[12])) {
+            h.ox = r[14]; h.oy = r[15]; h.is1 = r[16]; h.is2 = r[17];
+          } else {
+            any = false;
+          }
+          if (any) {
+            const SwrDrawDesc& D = g.draws[__float_as_int(r[1])];
+            span_row(h, y, D.sc_minx, D.sc_maxx, sp.x, sp.y);
+          }
+        }
+        if ((flags & 3) == 1) sspan[k * TILE + row] = sp;
+        if (kCull) {
+          // leftmost start of a span reaching the tile, over the primitive's TILE rows
+          int lmin = (sp.x < sp.y && sp.y > ox) ? sp.x : 0x7fffffff;
+#pragma unroll
+          for (int o = TILE / 2; o; o >>= 1) lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+          if (row == 0 && lmin != 0x7fffffff) atomicMin(&sminx[k], lmin);
+        }
+      }
+      __syncthreads();
+      // B1 (Span mode) masks from the spans: each row's [xl, xr) clipped to the block
+      for (int i = threadIdx.x; i < n * NB; i += 256) {
+        const int k = i / NB, j = i - k * NB;
+        const float* r = srec + k * RL::R;
+        const int flags = __float_as_int(r[0]);
+        if ((flags & 3) != 1) continue;
+        const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
+        const bool hit = bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
+                         by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]);
+        uint64_t m = 0;
+        if (hit) {
+#pragma unroll
+          for (int rr = 0; rr < SWR_BLOCK; ++rr) {
+            const int2 sp = sspan[k * TILE + (by - oy) + rr];
+            const int c0b = max(sp.x, bx) - bx, c1b = min(sp.y, bx + SWR_BLOCK) - bx;
+            if (c1b > c0b) m |= (((1ull << (c1b - c0b)) - 1ull) << c0b) << (rr * 8);
+          }
+        }
+        smask[i] = m;
+      }
+    } else {
+      __syncthreads();
+    }
     // B2: partially covered blocks, one row per lane (8 lanes per block)
     {
       const int np8 = (int)snpart * SWR_BLOCK;
@@ -1420,7 +1451,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             // whose span reaches the tile) to the pixel
             int steps = 2 * (SWR_BLOCK - 1);
             float X = (float)x1 + 0.5f;
-            if (!(__float_as_int(r[0]) & 2)) {
+            if (SPAN && !(__float_as_int(r[0]) & 2)) {
               const int smin = sminx[k];
               steps = max(0, x1 - smin);
               if (smin < 0) X = fmaxf(X, (float)(-smin) + 0.5f);
@@ -1534,7 +1565,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       const int x = ox + (blkj % NBX) * SWR_BLOCK + (bit & 7);
       const int y = oy + (blkj / NBX) * SWR_BLOCK + (bit >> 3);
       const float* r = srec + k * RL::R;
-      const bool blockmode = __float_as_int(r[0]) & 2;
+      const bool blockmode = !SPAN || (__float_as_int(r[0]) & 2);
       float fx, fy;
       int ka, kb;
       if (blockmode) {
@@ -1647,7 +1678,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
           PS::apply(st[q], sfz[f], sfc[f], prim_id(g, r, sids[k]));
           continue;
         }
-        const bool blockmode = __float_as_int(r[0]) & 2;
+        const bool blockmode = !SPAN || (__float_as_int(r[0]) & 2);
         float fx, fy;
         int ka, kb;
         if (blockmode) {
