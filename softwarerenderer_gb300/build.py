@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libswr_gb300.so")
-SOURCES = ["swr_core.cu", "swr_vs.cu", "swr_ps.cu", "swr_capi.cu", "swr_noalloc.cu", "swr_backward.cu", "swr_texture.cu", "swr_obj.cpp", "swr_image.cpp", "swr_target.cu"]
+SOURCES = ["swr_core.cu", "swr_vs.cu", "swr_ps.cu", "swr_ps_lambert.cu", "swr_ps_color.cu", "swr_ps_tex.cu", "swr_ps_deriv.cu", "swr_capi.cu", "swr_noalloc.cu", "swr_backward.cu", "swr_texture.cu", "swr_obj.cpp", "swr_image.cpp", "swr_target.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-ftz=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

@@ -1,0 +1,16 @@
+// PsOps of PsDiff, PsPerspDeriv.
+#include "swr_ps_impl.cuh"
+
+namespace swr {
+
+const PsOps* ps_ops_deriv(int id) {
+  static const PsOps kPsDiff = make<PsDiff>();
+  static const PsOps kPsPerspDeriv = make<PsPerspDeriv>();
+  switch (id) {
+    case SWR_PS_DIFF: return &kPsDiff;
+    case SWR_PS_PERSP_DERIV: return &kPsPerspDeriv;
+    default: return nullptr;
+  }
+}
+
+}  // namespace swr

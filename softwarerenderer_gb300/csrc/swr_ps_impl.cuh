@@ -1,0 +1,101 @@
+// Raster-stage kernels of the built-in pixel shaders: the launch wrappers and the PsOps table
+// entry of one shader, instantiated per shader in the swr_ps_*.cu translation units (split
+// so that the build compiles them in parallel).
+#pragma once
+#include "swr_ops.h"
+
+namespace swr {
+namespace {
+
+constexpr int kGrid = 152 * 8;
+constexpr int kChunk = SWR_CHUNK;  // primitives staged in shared memory per bin chunk
+
+template <class PS>
+void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {
+  if (!n) return;
+  const uint32_t want = (n + 255) / 256;
+  const int grid = (int)(want < (uint32_t)kGrid ? want : (uint32_t)kGrid);
+  k_direct_vertices<PS::AVarCount, PS::PVarCount><<<grid, 256, 0, s>>>(rv, n, ptv);
+}
+
+template <class PS>
+void run_setup(const SetupArgs& a, cudaStream_t s) {
+  k_setup<PS><<<kGrid, kSetupThreads, 0, s>>>(a);
+}
+
+template <class PS>
+void run_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+               const uint32_t* pair_off, const uint32_t* npairs, uint32_t cap_pairs,
+               const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* keys,
+               uint32_t* vals, uint32_t* status_w, cudaStream_t s) {
+  k_emit_pairs<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, pair_off, npairs, cap_pairs,
+                                         draws, targets, tile, keys, vals, status_w);
+}
+
+template <class PS>
+void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+              uint32_t* cell_count, const uint32_t* cell_start, uint32_t ncells, int seg_shift, uint32_t cap_pairs,
+              const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* bin, uint32_t* status_w,
+              cudaStream_t s) {
+  k_fill_bins<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, cell_count, cell_start, ncells,
+                                        seg_shift, cap_pairs, draws, targets, tile, bin, status_w);
+}
+
+template <class PS>
+void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
+  if (!ntiles) return;
+  // persistent grid: as many CTAs as fit at once (4 per SM), pulling tiles from the counter
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      nsm = 152;
+  }
+  const uint32_t grid = a.tile_counter ? (ntiles < (uint32_t)nsm * 4u ? ntiles : (uint32_t)nsm * 4u) : ntiles;
+  // Block-only submissions run the instantiation without the Span-mode passes
+  if (tile == 32) {
+    if (a.has_span) k_raster<PS, 32, kChunk, true><<<grid, 256, 0, s>>>(a);
+    else k_raster<PS, 32, kChunk, false><<<grid, 256, 0, s>>>(a);
+  } else {
+    if (a.has_span) k_raster<PS, 16, kChunk, true><<<grid, 256, 0, s>>>(a);
+    else k_raster<PS, 16, kChunk, false><<<grid, 256, 0, s>>>(a);
+  }
+}
+
+template <class PS>
+void run_lp_setup(const SetupArgs& a, cudaStream_t s) {
+  k_lp_setup<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+void run_lp_frags(const LpFragArgs& a, cudaStream_t s) {
+  k_lp_frags<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+void run_lp_shade(const LpShadeArgs& a, cudaStream_t s) {
+  k_lp_shade<PS><<<kGrid, 256, 0, s>>>(a);
+}
+
+template <class PS>
+PsOps make() {
+  PsOps o;
+  o.A = PS::AVarCount;
+  o.P = PS::PVarCount;
+  o.R = Rec<PS>::R;
+  o.S = VLayout<PS::AVarCount, PS::PVarCount>::S;
+  o.direct_vertices = &run_direct<PS>;
+  o.setup = &run_setup<PS>;
+  o.emit_pairs = &run_pairs<PS>;
+  o.raster = &run_raster<PS>;
+  o.fill_bins = &run_fill<PS>;
+  o.lp_R = LpRec<PS>::R;
+  o.lp_setup = &run_lp_setup<PS>;
+  o.lp_frags = &run_lp_frags<PS>;
+  o.lp_shade = &run_lp_shade<PS>;
+  o.needs_eq = SwrNeedsEquations<PS>::value;
+  return o;
+}
+
+}  // namespace
+}  // namespace swr

@@ -1,0 +1,16 @@
+// PsOps of PsLambert, PsLambertTex.
+#include "swr_ps_impl.cuh"
+
+namespace swr {
+
+const PsOps* ps_ops_lambert(int id) {
+  static const PsOps kPsLambert = make<PsLambert>();
+  static const PsOps kPsLambertTex = make<PsLambertTex>();
+  switch (id) {
+    case SWR_PS_LAMBERT: return &kPsLambert;
+    case SWR_PS_LAMBERT_TEX: return &kPsLambertTex;
+    default: return nullptr;
+  }
+}
+
+}  // namespace swr
