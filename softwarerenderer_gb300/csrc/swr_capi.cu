@@ -315,9 +315,6 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.draw_prim_base = c->use_draw_pbase ? c->draw_pbase.as<uint32_t>() : nullptr;
   ra.status_w = st;
   ra.ntiles = ntiles;
-  // one CTA per tile: a persistent grid pulling tiles from a counter measured no faster on
-  // the dense mesh and slower where few tiles carry the work (they gather on fewer SMs)
-  ra.tile_counter = nullptr;
   ra.has_span = has_span ? 1 : 0;
   ps->raster(ra, ntiles, c->tile, s);
   mark(c, 5, s);

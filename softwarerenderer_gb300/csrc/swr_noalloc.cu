@@ -215,7 +215,6 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.draw_prim_base = nullptr;
   ra.status_w = st;
   ra.ntiles = ntiles;
-  ra.tile_counter = nullptr;  // one CTA per tile
   ra.has_span = raster_mode != SWR_RASTER_BLOCK;
   ps->raster(ra, ntiles, kTile, s);
   uint32_t h[16];

@@ -44,14 +44,7 @@ void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs, con
 template <class PS>
 void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
   if (!ntiles) return;
-  // persistent grid: as many CTAs as fit at once (4 per SM), pulling tiles from the counter
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      nsm = 152;
-  }
-  const uint32_t grid = a.tile_counter ? (ntiles < (uint32_t)nsm * 4u ? ntiles : (uint32_t)nsm * 4u) : ntiles;
+  const uint32_t grid = ntiles;  // one CTA per tile
   // Block-only submissions run the instantiation without the Span-mode passes
   if (tile == 32) {
     if (a.has_span) k_raster<PS, 32, kChunk, true><<<grid, 256, 0, s>>>(a);

@@ -1022,7 +1022,6 @@ struct RasterArgs {
   const uint32_t* draw_prim_base;    // per draw first primitive (null: a single draw from 0)
   uint32_t* status_w;
   uint32_t ntiles;
-  uint32_t* tile_counter;            // optional: persistent grid's next-tile counter (starts at 0)
   int has_span;                      // some draw rasterizes in Span or Adaptive mode (selects k_raster<..., true>)
 };
 
@@ -1204,7 +1203,6 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   __shared__ uint32_t ssorted[SWR_RASTER_SORT];  // the tile's ordered bin (self-sorted tiles)
   __shared__ uint32_t scs[SWR_SEGS + 1];          // its cell starts relative to the bin start
   static_assert(sizeof(srec4) >= SWR_RASTER_SORT * 4, "raw bin staging fits the record area");
-  __shared__ uint32_t stile;
   constexpr bool kCull = SWR_DEPTH_CULL && SwrDepthCull<PS>::value;
   // Depth cull regions: the 8 x 4 pixels of one warp in one sub-tile (region q * 8 + warp).
   constexpr int NREG = 8 * PPT;
@@ -1217,27 +1215,12 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
-  // Tiles come from g.tile_counter (persistent grid: thread 0 claims the next non-empty
-  // tile in index order) or, without a counter, one tile per CTA (blockIdx.x).
-  for (uint32_t iter = 0;; ++iter) {
-  uint32_t tile = blockIdx.x;
-  if (g.tile_counter) {
-    __syncthreads();  // the previous tile's shared state is no longer read
-    if (threadIdx.x == 0) {
-      uint32_t t;
-      do {
-        t = atomicAdd(g.tile_counter, 1u);
-      } while (t < g.ntiles && g.tile_start[(size_t)t * g.tile_stride] == g.tile_start[(size_t)(t + 1) * g.tile_stride]);
-      stile = t;
-    }
-    __syncthreads();
-    tile = stile;
-  } else if (iter) {
-    break;
-  }
-  if (tile >= g.ntiles) break;
+  // one CTA per tile (a persistent grid pulling tiles from a counter measured no faster on
+  // the dense mesh and slower where few tiles carry the work: they gather on fewer SMs)
+  const uint32_t tile = blockIdx.x;
+  if (tile >= g.ntiles) return;
   const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
-  if (b == e) continue;  // uniform per CTA
+  if (b == e) return;  // uniform per CTA
   const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
   const SwrTargetDesc& T = g.targets[ti];
   const SwrUniforms& U = g.draws[T.first_draw].u;
@@ -1711,7 +1694,6 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       PS::store(st[q], px[q], py[q], U);
       passes += st[q].writes;
     }
-  }  // tiles
   // fragment statistics: drawPixel calls and colour writes
   uint32_t tot, ptot;
   swr_block_exscan(frags, sfr, &tot);
