@@ -107,6 +107,8 @@ struct swr_context {
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
   swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
   swr::Buffer big_cells;  // k_sort_cells -> k_sort_big: [count, cell ids...]
+  swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
+  int slices = 1;           // slices the buffer holds for the current tile count
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
   int32_t* prim_src = nullptr;  // swr_set_primitive_source
   uint64_t prim_src_cap = 0;
@@ -176,7 +178,7 @@ bool grow_u32(uint32_t& cap, uint64_t need) {
 
 // Allocates every queue a draw with the given host-known sizes needs.
 int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, uint32_t nbatches,
-                    uint32_t ntiles, int R) {
+                    uint32_t ntiles, int R, const PsOps* ps) {
   grow_u32(c->cap_prims, (uint64_t)nsub + 1024);
   grow_u32(c->cap_clip_slots, (uint64_t)nsub / 16 + 1024);
   grow_u32(c->cap_clip_verts, (uint64_t)c->cap_clip_slots * 4);
@@ -209,6 +211,15 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
     ok &= c->big_cells.ensure(((size_t)ntiles * SWR_SEGS + 2) * 4 + 16);
     // the list length and completion counter start at zero (k_sort_big resets them)
     ok &= c->big_cells.p && cudaMemset(c->big_cells.p, 0, 8) == cudaSuccess;
+  }
+  // Overwrite shaders: tiles of many layers are rasterized in up to SWR_SLICES_MAX slices
+  // (the buffer is kept under 512 MiB by using fewer slices on large targets).
+  c->slices = 1;
+  if (ps && ps->overwrite) {
+    const size_t per_slice = (size_t)ntiles * c->tile * c->tile * (size_t)ps->state_bytes;
+    int k = SWR_SLICES_MAX;
+    while (k > 1 && per_slice * (size_t)k > ((size_t)512 << 20)) --k;
+    if (k > 1 && c->slice_state.ensure(per_slice * (size_t)k)) c->slices = k;
   }
   const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64 + 2 * scan_scratch_words(ntiles * SWR_SEGS);
   ok &= c->scratch.ensure(sw * 4);
@@ -316,7 +327,10 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.status_w = st;
   ra.ntiles = ntiles;
   ra.has_span = has_span ? 1 : 0;
+  ra.slices = ps->overwrite ? c->slices : 1;
+  ra.slice_state = c->slice_state.p;
   ps->raster(ra, ntiles, c->tile, s);
+  if (ra.slices > 1) c->launches += 1;  // k_merge_slices
   mark(c, 5, s);
   if (!use_big) {
     k_close_draw<<<1, 1, 0, s>>>(st);
@@ -599,7 +613,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   const uint32_t nbatches = (nsub + SWR_BATCH_PRIMS - 1) / SWR_BATCH_PRIMS;
   const SwrTargetDesc T = make_target(c);
   const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
-  int rc = ensure_capacity(c, (uint32_t)nverts, vs->S, nsub, nbatches, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R);
+  int rc = ensure_capacity(c, (uint32_t)nverts, vs->S, nsub, nbatches, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R, ps);
   if (rc) return rc;
   SwrDrawDesc D;
   fill_draw(c, D, mode);
@@ -661,7 +675,7 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   const uint32_t nsub = (uint32_t)(count / per);
   const SwrTargetDesc T = make_target(c);
   const uint32_t ntiles = (uint32_t)T.tiles_x * (uint32_t)T.tiles_y;
-  int rc = ensure_capacity(c, (uint32_t)nverts, ps->S, nsub, 1, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R);
+  int rc = ensure_capacity(c, (uint32_t)nverts, ps->S, nsub, 1, ntiles, ps->R > ps->lp_R ? ps->R : ps->lp_R, ps);
   if (rc) return rc;
   if (!c->direct_keep.ensure((size_t)nsub * 4 + 16) || !c->direct_pos.ensure((size_t)nsub * 4 + 16))
     return SWR_ENOMEM;
@@ -793,7 +807,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     return SWR_EINVAL;
   const int ntg = (int)T.size();
   int rc = ensure_capacity(c, (uint32_t)V, vs->S, (uint32_t)P, (uint32_t)B, (uint32_t)NT,
-                           ps->R > ps->lp_R ? ps->R : ps->lp_R);
+                           ps->R > ps->lp_R ? ps->R : ps->lp_R, ps);
   if (rc) return rc;
   bool ok = c->draws.ensure(sizeof(SwrDrawDesc) * n) && c->targets.ensure(sizeof(SwrTargetDesc) * ntg) &&
             c->draw_vbase.ensure(4 * n + 16) && c->draw_bbase.ensure(4 * n + 16) && c->draw_pbase.ensure(4 * n + 16) &&
@@ -826,7 +840,8 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
                         c->tris.p, c->recs.p, c->tile_count.p, c->keys0.p, c->vals0.p, c->cell_count.p,
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
-                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage};
+                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage,
+                        c->slice_state.p, (const void*)(uintptr_t)c->slices};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
   if (c->graph_mode && c->gexec && sig == c->gsig) {
     if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;

@@ -15,6 +15,8 @@
 #define SWR_RASTER_MINB 0         // k_raster CTAs per SM to plan registers for (0: per shader)
 #endif
 #define SWR_RASTER_SORT 512       // tiles with at most this many bin entries are ordered by k_raster
+#define SWR_SLICES_MAX 8          // overwrite shaders: CTAs (ordered bin slices) per tile of more than
+                                  // SWR_RASTER_SORT entries, merged by k_merge_slices
 #ifndef SWR_DEPTH_CULL
 #define SWR_DEPTH_CULL 1          // k_raster's per-chunk tile depth cull (depth-tested shaders)
 #endif

@@ -216,6 +216,8 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.status_w = st;
   ra.ntiles = ntiles;
   ra.has_span = raster_mode != SWR_RASTER_BLOCK;
+  ra.slices = 1;  // no slice buffer without allocation
+  ra.slice_state = nullptr;
   ps->raster(ra, ntiles, kTile, s);
   uint32_t h[16];
   if (cudaMemcpyAsync(h, st, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

@@ -35,6 +35,8 @@ struct PsOps {
   void (*lp_frags)(const LpFragArgs& a, cudaStream_t s);
   void (*lp_shade)(const LpShadeArgs& a, cudaStream_t s);
   int needs_eq;  // shade() reads the triangle equations: triangles only
+  int overwrite;    // SwrOverwrite: large tiles may be rasterized in slices (RasterArgs.slices)
+  int state_bytes;  // sizeof(PS::State), per pixel and slice of RasterArgs.slice_state
 };
 
 const VsOps* vs_ops(int id);

@@ -685,6 +685,18 @@ struct SwrDepthCull<PS, decltype((void)PS::DepthCull)> {
   enum { value = PS::DepthCull && PS::HasDepth && PS::InterpolateZ && !SwrOverwrite<PS>::value };
 };
 
+// Overwrite shaders' State after two consecutive runs of fragments: the later run's last
+// writer (colour, winner) if it wrote at all, and the summed counters.  Lets a rasterizer
+// split one pixel's fragments into ordered slices and merge their states.
+SWR_HD void swr_overwrite_merge(SwrStateRGBA8& acc, const SwrStateRGBA8& later) {
+  if (later.writes) {
+    acc.color = later.color;
+    acc.winner = later.winner;
+  }
+  acc.frags += later.frags;
+  acc.writes += later.writes;
+}
+
 // Resident tile-raster CTAs per SM the register allocation of a shader's k_raster must
 // allow (RasterOccupancy in the shader; measured per workload, default 4).
 template <class PS, class = void>

@@ -44,14 +44,20 @@ void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs, con
 template <class PS>
 void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
   if (!ntiles) return;
-  const uint32_t grid = ntiles;  // one CTA per tile
-  // Block-only submissions run the instantiation without the Span-mode passes
+  // one CTA per tile, or per (tile, slice) for sliced overwrite shaders; Block-only
+  // submissions run the instantiation without the Span-mode passes
+  const bool sliced = SwrOverwrite<PS>::value && a.slices > 1;
+  const uint32_t grid = sliced ? ntiles * (uint32_t)a.slices : ntiles;
   if (tile == 32) {
     if (a.has_span) k_raster<PS, 32, kChunk, true><<<grid, 256, 0, s>>>(a);
     else k_raster<PS, 32, kChunk, false><<<grid, 256, 0, s>>>(a);
+    if constexpr (SwrOverwrite<PS>::value)
+      if (sliced) k_merge_slices<PS, 32><<<ntiles, 256, 0, s>>>(a);
   } else {
     if (a.has_span) k_raster<PS, 16, kChunk, true><<<grid, 256, 0, s>>>(a);
     else k_raster<PS, 16, kChunk, false><<<grid, 256, 0, s>>>(a);
+    if constexpr (SwrOverwrite<PS>::value)
+      if (sliced) k_merge_slices<PS, 16><<<ntiles, 256, 0, s>>>(a);
   }
 }
 
@@ -87,6 +93,8 @@ PsOps make() {
   o.lp_frags = &run_lp_frags<PS>;
   o.lp_shade = &run_lp_shade<PS>;
   o.needs_eq = SwrNeedsEquations<PS>::value;
+  o.overwrite = SwrOverwrite<PS>::value;
+  o.state_bytes = (int)sizeof(typename PS::State);
   return o;
 }
 

@@ -1022,6 +1022,9 @@ struct RasterArgs {
   const uint32_t* draw_prim_base;    // per draw first primitive (null: a single draw from 0)
   uint32_t* status_w;
   uint32_t ntiles;
+  int slices;                        // overwrite shaders: CTAs per tile of more than SWR_RASTER_SORT
+                                     // entries (1: no slicing), each over an ordered slice of its bin
+  void* slice_state;                 // their per-pixel PS::State, [tile][slice][TILE * TILE]
   int has_span;                      // some draw rasterizes in Span or Adaptive mode (selects k_raster<..., true>)
 };
 
@@ -1215,12 +1218,35 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
-  // one CTA per tile (a persistent grid pulling tiles from a counter measured no faster on
-  // the dense mesh and slower where few tiles carry the work: they gather on fewer SMs)
-  const uint32_t tile = blockIdx.x;
+  // One CTA per tile (a persistent grid pulling tiles from a counter measured no faster on
+  // the dense mesh and slower where few tiles carry the work: they gather on fewer SMs).
+  // Overwrite shaders with g.slices > 1: CTA (tile, slice); a tile of more than
+  // SWR_RASTER_SORT entries (an ordered bin) is cut into g.slices runs of whole chunks, each
+  // rasterized from an empty State into slice_state and merged in order by k_merge_slices;
+  // smaller tiles are rasterized whole by slice 0.
+  uint32_t tile = blockIdx.x, slice = 0;
+  if (SwrOverwrite<PS>::value && g.slices > 1) {
+    tile = blockIdx.x / (uint32_t)g.slices;
+    slice = blockIdx.x - tile * (uint32_t)g.slices;
+  }
   if (tile >= g.ntiles) return;
-  const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
-  if (b == e) return;  // uniform per CTA
+  uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
+  bool sliced = false;
+  if constexpr (SwrOverwrite<PS>::value) {
+    if (g.slices > 1) {
+      if (e - b <= (uint32_t)SWR_RASTER_SORT) {
+        if (slice) return;
+      } else {
+        sliced = true;
+        const uint32_t nch = (e - b + CH - 1) / CH, ns = (uint32_t)g.slices;
+        const uint32_t lo = b + (uint32_t)((uint64_t)nch * slice / ns) * CH;
+        const uint32_t hi = min(e, b + (uint32_t)((uint64_t)nch * (slice + 1) / ns) * CH);
+        b = lo;
+        e = hi > lo ? hi : lo;  // an empty slice still writes its (empty) states
+      }
+    }
+  }
+  if (b == e && !sliced) return;  // uniform per CTA
   const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
   const SwrTargetDesc& T = g.targets[ti];
   const SwrUniforms& U = g.draws[T.first_draw].u;
@@ -1245,7 +1271,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   // A tile of at most SWR_RASTER_SORT entries orders its own bin: the cells (increasing id
   // segments) are contiguous, so an id's position is its cell's start plus the number of
   // smaller ids in that cell.  The raw ids are staged in the record area (used only later).
-  const bool self_sort = g.bin_raw && e - b <= (uint32_t)SWR_RASTER_SORT;
+  const bool self_sort = g.bin_raw && !sliced && e - b <= (uint32_t)SWR_RASTER_SORT;
   if (self_sort) {
     uint32_t* sraw = (uint32_t*)srec4;
     const uint32_t ntot = e - b;
@@ -1691,7 +1717,13 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 #pragma unroll
   for (int q = 0; q < PPT; ++q)
     if (in[q]) {
-      PS::store(st[q], px[q], py[q], U);
+      if (sliced) {
+        typename PS::State* ss = (typename PS::State*)g.slice_state +
+                                 ((size_t)tile * g.slices + slice) * (TILE * TILE);
+        ss[(py[q] - oy) * TILE + (px[q] - ox)] = st[q];
+      } else {
+        PS::store(st[q], px[q], py[q], U);
+      }
       passes += st[q].writes;
     }
   // fragment statistics: drawPixel calls and colour writes
@@ -1701,6 +1733,34 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   if (threadIdx.x == 0 && tot) {
     atomicAdd((unsigned long long*)&g.status_w[SWR_ST_SHADED_LO], (unsigned long long)tot);
     atomicAdd((unsigned long long*)&g.status_w[SWR_ST_PASSES_LO], (unsigned long long)ptot);
+  }
+}
+
+// Merges the slices of the tiles k_raster sliced (more than SWR_RASTER_SORT entries):
+// per pixel the slices' States in bin order (swr_overwrite_merge), then the shader's store.
+template <class PS, int TILE>
+__global__ void __launch_bounds__(256) k_merge_slices(RasterArgs g) {
+  constexpr int PPT = TILE * TILE / 256;
+  if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= g.ntiles) return;
+  const uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
+  if (e - b <= (uint32_t)SWR_RASTER_SORT) return;
+  const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
+  const SwrTargetDesc& T = g.targets[ti];
+  const SwrUniforms& U = g.draws[T.first_draw].u;
+  const uint32_t lt = tile - T.tile_base;
+  const int ox = (int)(lt % (uint32_t)T.tiles_x) * TILE, oy = (int)(lt / (uint32_t)T.tiles_x) * TILE;
+  const typename PS::State* ss = (const typename PS::State*)g.slice_state + (size_t)tile * g.slices * (TILE * TILE);
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) {
+    const int i = q * 256 + threadIdx.x;
+    const int x = ox + i % TILE, y = oy + i / TILE;
+    if (x >= T.width || y >= T.height) continue;
+    typename PS::State m;
+    PS::load(m, x, y, U);
+    for (int sl = 0; sl < g.slices; ++sl) swr_overwrite_merge(m, ss[(size_t)sl * (TILE * TILE) + i]);
+    PS::store(m, x, y, U);
   }
 }
 

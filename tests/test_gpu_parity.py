@@ -166,3 +166,15 @@ def test_dense_soup_all_modes(gpu_lib, port, mode):
     st = _check(port, sc)
     assert st["fragments"] > 20 * 320 * 240
     _check_prefilled(port, sc, 5)
+
+
+@pytest.mark.parametrize("n_tris", [1000, 3000, 8000])
+@pytest.mark.parametrize("mode", [RasterMode.Span, RasterMode.Block, RasterMode.Adaptive])
+def test_overwrite_sliced_tiles(gpu_lib, port, n_tris, mode):
+    """Overwrite shader (no depth test) with hundreds to thousands of primitives per tile:
+    tiles above the in-kernel sort limit are rasterized in ordered slices by separate CTAs
+    and merged (last writer, summed counts); smaller tiles stay whole."""
+    sc = scenes.benchmark_scene(n_tris, seed=7)
+    sc.raster = mode
+    st = _check(port, sc)
+    assert st["fragments"] > 0
