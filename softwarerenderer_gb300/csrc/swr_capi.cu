@@ -291,7 +291,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   uint32_t* scr = c->scratch.as<uint32_t>();
   uint32_t* cstart = c->cell_start.as<uint32_t>();
   scan_exclusive(c->cell_count.as<uint32_t>(), cstart, nullptr, ncells, cstart + ncells, scr, s);
-  ps->fill_bins(st, c->cap_prims, c->recs.as<float>(), c->tile_count.as<uint32_t>(), c->cell_count.as<uint32_t>(),
+  ps->fill_bins(st, c->cap_prims, c->recs.as<float>(), c->cell_count.as<uint32_t>(),
                 cstart, ncells, seg_shift, c->cap_pairs, c->draws.as<SwrDrawDesc>(), c->targets.as<SwrTargetDesc>(),
                 c->tile, c->keys0.as<uint32_t>(), st, s);
   const uint32_t warps_per_block = 8;

@@ -26,7 +26,7 @@ struct PsOps {
                      uint32_t cap_pairs, const SwrDrawDesc* draws, const SwrTargetDesc* targets,
                      int tile, uint32_t* keys, uint32_t* vals, uint32_t* status_w, cudaStream_t s);
   void (*raster)(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s);
-  void (*fill_bins)(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+  void (*fill_bins)(const uint32_t* status, uint32_t cap_prims, const float* recs,
                     uint32_t* cell_count, const uint32_t* cell_start, uint32_t ncells, int seg_shift,
                     uint32_t cap_pairs, const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile,
                     uint32_t* bin, uint32_t* status_w, cudaStream_t s);

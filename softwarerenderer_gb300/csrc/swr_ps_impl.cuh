@@ -33,11 +33,11 @@ void run_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs, co
 }
 
 template <class PS>
-void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs, const uint32_t* tile_count,
+void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs,
               uint32_t* cell_count, const uint32_t* cell_start, uint32_t ncells, int seg_shift, uint32_t cap_pairs,
               const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* bin, uint32_t* status_w,
               cudaStream_t s) {
-  k_fill_bins<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, cell_count, cell_start, ncells,
+  k_fill_bins<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, cell_count, cell_start, ncells,
                                         seg_shift, cap_pairs, draws, targets, tile, bin, status_w);
 }
 

@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(256) k_emit_pairs(const uint32_t* status, uint
 // the fill order is arbitrary and k_sort_cells restores increasing primitive order.
 template <class PS>
 __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint32_t cap_prims, const float* recs,
-                                                   const uint32_t* tile_count, uint32_t* cell_count,
+                                                   uint32_t* cell_count,
                                                    const uint32_t* cell_start, uint32_t ncells, int seg_shift,
                                                    uint32_t cap_pairs, const SwrDrawDesc* draws,
                                                    const SwrTargetDesc* targets, int tile, uint32_t* bin,
