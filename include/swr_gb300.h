@@ -129,6 +129,22 @@ int swr_set_graph_mode(swr_context* ctx, int on);
 
 /* Wait for the stream, report and reset the accumulated status. */
 int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
+/* Queue sizes (no reference counterpart: the reference grows std::vectors).  A context
+ * sizes its primitive queue (triangles after clipping and culling) and its bin-entry queue
+ * ((tile, primitive) pairs) ahead of every draw from the submitted count; a draw that
+ * needs more is skipped on the device, swr_finish returns SWR_EOVERFLOW with the targets
+ * untouched and grows the queue to what the draw asked for, and the caller draws again.
+ * swr_set_queue_capacity fixes either size instead (0 keeps the automatic sizing): a
+ * caller that knows its scenes (an autotuned batch) pre-sizes the queues once; they are
+ * still grown after an overflow.  swr_get_queue_capacity reports the current sizes. */
+int swr_set_queue_capacity(swr_context* ctx, uint64_t primitives, uint64_t bin_entries);
+int swr_get_queue_capacity(swr_context* ctx, uint64_t* primitives, uint64_t* bin_entries);
+/* Device-memory budget (no reference counterpart): the context's scratch allocations
+ * fail with SWR_ENOMEM, queuing nothing, once they would hold more than `bytes` (0: no
+ * limit, the default), exactly as when cudaMalloc itself fails; swr_memory_used reports
+ * the bytes held. */
+int swr_set_memory_limit(swr_context* ctx, uint64_t bytes);
+int swr_memory_used(swr_context* ctx, uint64_t* bytes);
 /* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels. */
 int swr_set_tile_size(swr_context* ctx, int tile);
 const char* swr_status_string(int status);
@@ -247,9 +263,12 @@ int swr_write_image(const char* path, const void* pixels, int width, int height,
  * of 16 x 16 pixels (e.g. 2048 x 2048); larger inputs return SWR_EINVAL up front, and more
  * than 262144 (tile, triangle) bin entries return SWR_EOVERFLOW with the target untouched.
  * Synchronous: returns after the stream has drained; *fragments (may be NULL) receives
- * the drawPixel count.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) and must come before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race, so serialise them. */
+ * the drawPixel count.  The first call on a device is its set-up: it looks up the array's
+ * address (cudaGetSymbolAddress), and under lazy module loading (the CUDA default) it is
+ * also when the library's device code and the 8 MiB array are loaded, the one call that
+ * can allocate -- make it once at start-up, before any stream capture.  After
+ * cudaDeviceReset the next call repeats the set-up in the new context.  All calls share
+ * the array: calls that overlap on the GPU race, so serialise them. */
 int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int ps_id, int raster_mode,
                                    int scissor_x, int scissor_y, int scissor_w, int scissor_h,
                                    const float* vertices, uint64_t nverts,

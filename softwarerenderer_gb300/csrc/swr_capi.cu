@@ -52,23 +52,34 @@ __global__ void k_stage_copy(const StageCopy sc) {
 
 __global__ void k_close_draw(uint32_t* st) { swr_close_status(st); }
 
+// Device bytes a context holds, and the cap swr_set_memory_limit puts on them (0: none).
+struct MemBudget {
+  size_t used = 0;
+  size_t limit = 0;
+};
+
 struct Buffer {
   void* p = nullptr;
   size_t bytes = 0;
+  MemBudget* budget = nullptr;
   ~Buffer() {
     if (p) cudaFree(p);
   }
   bool ensure(size_t n) {
     if (n <= bytes) return true;
+    size_t want = n + n / 4;
+    // over the context's budget: fail like an allocation failure, keeping the old buffer
+    if (budget && budget->limit && budget->used - bytes + want > budget->limit) return false;
     if (p) cudaFree(p);
+    if (budget) budget->used -= bytes;
     p = nullptr;
     bytes = 0;
-    size_t want = n + n / 4;
     if (cudaMalloc(&p, want) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
     bytes = want;
+    if (budget) budget->used += want;
     return true;
   }
   template <class T>
@@ -114,6 +125,10 @@ struct swr_context {
   uint64_t prim_src_cap = 0;
   uint32_t* status_host = nullptr;
   uint32_t last_ntiles = 0;
+  // swr_set_queue_capacity: queues sized by the caller are not grown ahead of a draw (only
+  // after a draw overflowed them); swr_set_memory_limit caps the device bytes held
+  bool fixed_prims = false, fixed_pairs = false;
+  swr::MemBudget budget;
   // tracing: CUDA events at the stage boundaries of every draw since the last
   // swr_stage_times call (swr_set_profiling); sextuples reused from a pool
   bool profiling = false;
@@ -136,6 +151,15 @@ struct swr_context {
   cudaStream_t cap_stream = nullptr;  // graphs are recorded here, then launched on the caller's stream
   uint64_t gsig = 0;
   uint64_t glaunches = 0;  // kernels per replay of the cached graph
+
+  void attach_budget() {
+    swr::Buffer* all[] = {&draws, &targets, &draw_vbase, &draw_bbase, &target_tile_base, &ptv, &clipv,
+                          &clip_table, &clip_slot, &tri_flags, &batch_counts, &batch_base, &tris, &recs,
+                          &tile_count, &pair_off, &keys0, &vals0, &keys1, &vals1, &tile_start, &scratch,
+                          &status, &direct_keep, &direct_pos, &lp_refs, &cell_count, &cell_start, &draw_pbase,
+                          &big_cells, &slice_state};
+    for (swr::Buffer* b : all) b->budget = &budget;
+  }
 };
 
 namespace {
@@ -179,10 +203,10 @@ bool grow_u32(uint32_t& cap, uint64_t need) {
 // Allocates every queue a draw with the given host-known sizes needs.
 int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, uint32_t nbatches,
                     uint32_t ntiles, int R, const PsOps* ps) {
-  grow_u32(c->cap_prims, (uint64_t)nsub + 1024);
+  if (!c->fixed_prims) grow_u32(c->cap_prims, (uint64_t)nsub + 1024);
   grow_u32(c->cap_clip_slots, (uint64_t)nsub / 16 + 1024);
   grow_u32(c->cap_clip_verts, (uint64_t)c->cap_clip_slots * 4);
-  grow_u32(c->cap_pairs, (uint64_t)c->cap_prims * 2 + 65536);
+  if (!c->fixed_pairs) grow_u32(c->cap_pairs, (uint64_t)c->cap_prims * 2 + 65536);
   bool ok = true;
   ok &= c->ptv.ensure((size_t)nverts_ptv * S * 4 + 16);
   ok &= c->clipv.ensure((size_t)c->cap_clip_verts * S * 4 + 16);
@@ -463,6 +487,7 @@ int swr_create(swr_context** out) {
   if (!out) return SWR_EINVAL;
   swr_context* c = new swr_context();
   memset(&c->u, 0, sizeof(c->u));
+  c->attach_budget();
   // the segment bitmaps of k_sort_big may exceed the default 48 KB of dynamic shared memory
   cudaFuncSetAttribute(k_sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBigSortSmem);
   cudaGetLastError();
@@ -555,6 +580,34 @@ int swr_set_primitive_source(swr_context* c, int32_t* out, uint64_t capacity) {
   if (!c || (out && !capacity)) return SWR_EINVAL;
   c->prim_src = out;
   c->prim_src_cap = out ? capacity : 0;
+  return SWR_OK;
+}
+
+int swr_set_queue_capacity(swr_context* c, uint64_t primitives, uint64_t bin_entries) {
+  if (!c || primitives > 0xffffffffull || bin_entries > 0xffffffffull) return SWR_EINVAL;
+  c->fixed_prims = primitives != 0;
+  c->fixed_pairs = bin_entries != 0;
+  if (primitives) c->cap_prims = (uint32_t)primitives;
+  if (bin_entries) c->cap_pairs = (uint32_t)bin_entries;
+  return SWR_OK;
+}
+
+int swr_get_queue_capacity(swr_context* c, uint64_t* primitives, uint64_t* bin_entries) {
+  if (!c) return SWR_EINVAL;
+  if (primitives) *primitives = c->cap_prims;
+  if (bin_entries) *bin_entries = c->cap_pairs;
+  return SWR_OK;
+}
+
+int swr_set_memory_limit(swr_context* c, uint64_t bytes) {
+  if (!c) return SWR_EINVAL;
+  c->budget.limit = (size_t)bytes;
+  return SWR_OK;
+}
+
+int swr_memory_used(swr_context* c, uint64_t* bytes) {
+  if (!c || !bytes) return SWR_EINVAL;
+  *bytes = c->budget.used;
   return SWR_OK;
 }
 

@@ -17,11 +17,18 @@
 //   skipped and SWR_EOVERFLOW returned).  The array is 8 MiB and every GPU that loads
 //   the library holds it until the process exits.
 //
-// The first call on a device (with that device current) looks up the array's device
-// address with cudaGetSymbolAddress and caches it; make that first call before any
-// stream capture.  Every call shares the one array and leaves its contents behind; the
-// entry point clears what must start at zero itself.  Calls whose work overlaps on the
-// GPU (different streams, or different host threads) race on the array: serialise them.
+// Set-up: the first call on a device (with that device current) looks up the array's
+// device address with cudaGetSymbolAddress and caches it together with the id of the
+// current CUDA context; make that first call before any stream capture.  With lazy module
+// loading (the CUDA default) that first call is also when the library's device code and
+// the 8 MiB array are loaded onto the device, so it is the one call that can allocate:
+// a caller whose device memory is capped makes it once at start-up.  After the
+// application re-creates the device's context (cudaDeviceReset), the next call sees a new
+// context id and repeats the set-up.  Every call shares the one array and leaves its
+// contents behind; the entry point clears what must start at zero itself.  Calls whose
+// work overlaps on the GPU (different streams, or different host threads) race on the
+// array: serialise them.
+#include <cuda.h>  // CUcontext and CUresult only: the two driver calls are resolved at run time
 #include <mutex>
 #include <string.h>
 #include "../../include/swr_gb300.h"
@@ -78,22 +85,72 @@ Layout make_layout() {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-unsigned char* g_base[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (looked up once per device).
+// Per device: the scratch array's address and the id of the context it was looked up in.
+struct DeviceSlot {
+  unsigned long long ctx_id;
+  unsigned char* base;
+};
+DeviceSlot g_slot[kMaxDevices] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Id of the calling thread's current context (unique for the life of the process; 0 when
+// no context is current yet).  Caller holds g_mutex.
+int current_context_id(unsigned long long* id) {
+  *id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f)
+      return SWR_ECUDA;
+    g_ctx_get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f)
+      return SWR_ECUDA;
+    g_ctx_get_id = (CtxGetIdFn)f;
+  }
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return SWR_ECUDA;
+  if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return SWR_ECUDA;
+  return SWR_OK;
+}
+
+// Device address of the scratch array on the current device: looked up once per device
+// and again whenever the current context is not the one it was looked up in.
 int scratch_base(unsigned char** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SWR_ECUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return SWR_ECUDA;
+  }
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_base[dev]) {
+  unsigned long long id = 0;
+  if (current_context_id(&id)) {
+    cudaGetLastError();
+    return SWR_ECUDA;
+  }
+  DeviceSlot& slot = g_slot[dev];
+  if (!slot.base || !id || id != slot.ctx_id) {
     void* p = nullptr;
+    // makes the device's primary context current when no context was yet
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
       cudaGetLastError();
       return SWR_ECUDA;
     }
-    g_base[dev] = (unsigned char*)p;
+    if (current_context_id(&id) || !id) {
+      cudaGetLastError();
+      return SWR_ECUDA;
+    }
+    slot.base = (unsigned char*)p;
+    slot.ctx_id = id;
   }
-  *out = g_base[dev];
+  *out = slot.base;
   return SWR_OK;
 }
 
@@ -219,6 +276,7 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.slices = 1;  // no slice buffer without allocation
   ra.slice_state = nullptr;
   ps->raster(ra, ntiles, kTile, s);
+  if (cudaGetLastError() != cudaSuccess) return SWR_ECUDA;  // a launch failed: the status words are stale
   uint32_t h[16];
   if (cudaMemcpyAsync(h, st, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess) {

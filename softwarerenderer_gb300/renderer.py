@@ -59,6 +59,38 @@ class Context:
         self.L.swr_set_graph_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib.check(self.L.swr_set_graph_mode(self.h, int(bool(on))), "set_graph_mode")
 
+    def set_queue_capacity(self, primitives=0, bin_entries=0):
+        """Fix the primitive / bin-entry queue sizes (0: automatic); swr_set_queue_capacity."""
+        L = self.L
+        L.swr_set_queue_capacity.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64]
+        L.swr_set_queue_capacity.restype = ctypes.c_int
+        _lib.check(L.swr_set_queue_capacity(self.h, int(primitives), int(bin_entries)), "set_queue_capacity")
+
+    def queue_capacity(self):
+        L = self.L
+        L.swr_get_queue_capacity.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                             ctypes.POINTER(ctypes.c_uint64)]
+        L.swr_get_queue_capacity.restype = ctypes.c_int
+        p, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        _lib.check(L.swr_get_queue_capacity(self.h, ctypes.byref(p), ctypes.byref(b)), "queue_capacity")
+        return int(p.value), int(b.value)
+
+    def set_memory_limit(self, nbytes=0):
+        """Cap the device bytes the context's scratch may hold (0: no cap); beyond it draws
+        fail with SWR_ENOMEM and queue nothing."""
+        L = self.L
+        L.swr_set_memory_limit.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.swr_set_memory_limit.restype = ctypes.c_int
+        _lib.check(L.swr_set_memory_limit(self.h, int(nbytes)), "set_memory_limit")
+
+    def memory_used(self):
+        L = self.L
+        L.swr_memory_used.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.swr_memory_used.restype = ctypes.c_int
+        v = ctypes.c_uint64(0)
+        _lib.check(L.swr_memory_used(self.h, ctypes.byref(v)), "memory_used")
+        return int(v.value)
+
     def set_profiling(self, on=True):
         _lib.check(self.L.swr_set_profiling(self.h, int(bool(on))), "set_profiling")
 

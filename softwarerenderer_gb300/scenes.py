@@ -628,7 +628,20 @@ def scene_from_spec(spec: dict) -> Scene:
         return box_scene(spec["frame"])
     if k == "deriv":
         return deriv_scene(spec["frame"], raster=RasterMode(spec.get("raster", 0)))
+    if k == "batch":
+        return _batch_cached(spec.get("n", 256), spec.get("seed", 4))[spec["item"]]
     raise ValueError(k)
+
+
+_BATCH_CACHE = {}
+
+
+def _batch_cached(n, seed):
+    """batch_scenes(n, seed) built once per process (fixtures pick single items of it)."""
+    if (n, seed) not in _BATCH_CACHE:
+        _BATCH_CACHE.clear()
+        _BATCH_CACHE[(n, seed)] = batch_scenes(n, seed=seed)
+    return _BATCH_CACHE[(n, seed)]
 
 
 def scene_digest(scene: Scene) -> str:

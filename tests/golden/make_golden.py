@@ -38,6 +38,9 @@ def specs():
     # the Box example's mip-mapped anisotropic sampler, and the perspective derivatives
     out += [{"kind": "box", "frame": f} for f in range(16)]
     out += [{"kind": "deriv", "frame": f, "raster": m} for f in range(8) for m in (0, 1, 2)]
+    # items of the 256-mesh batched workload (scenes.batch_scenes(256)): the first four,
+    # the three smallest (103-108 triangles) and the three largest (193k-198k triangles)
+    out += [{"kind": "batch", "item": i} for i in (0, 1, 2, 3, 26, 98, 196, 79, 191, 69)]
     return out
 
 
