@@ -21,6 +21,15 @@
 
 #include <stdint.h>
 
+/* Every entry point is exported; the library's internal symbols (built with hidden
+ * visibility) are not, so kernels a caller instantiates from the same headers for its
+ * own shaders (include/swr/Renderer.h) never bind to the library's copies or vice versa. */
+#if defined(__GNUC__)
+#define SWR_API __attribute__((visibility("default")))
+#else
+#define SWR_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -61,39 +70,51 @@ typedef struct swr_stats {
 /* Context lifetime.  Replaces constructing VertexProcessor(IRasterizer*) + Rasterizer()
  * (VertexProcessor.cpp:29-35, Rasterizer.h:67-72): defaults are CullMode::CW, depth range
  * (0, 1), RasterMode::Span, scissor (0, 0, 0, 0), tile size 16. */
-int swr_create(swr_context** out);
-int swr_destroy(swr_context* ctx);
+SWR_API int swr_create(swr_context** out);
+SWR_API int swr_destroy(swr_context* ctx);
 
 /* VertexProcessor::setViewport (VertexProcessor.h:66, VertexProcessor.cpp:43-54). */
-int swr_set_viewport(swr_context* ctx, int x, int y, int width, int height);
+SWR_API int swr_set_viewport(swr_context* ctx, int x, int y, int width, int height);
 /* VertexProcessor::setDepthRange (VertexProcessor.h:70, VertexProcessor.cpp:56-60). */
-int swr_set_depth_range(swr_context* ctx, float n, float f);
+SWR_API int swr_set_depth_range(swr_context* ctx, float n, float f);
 /* VertexProcessor::setCullMode (VertexProcessor.h:74, VertexProcessor.cpp:62-65). */
-int swr_set_cull_mode(swr_context* ctx, int mode);
+SWR_API int swr_set_cull_mode(swr_context* ctx, int mode);
 /* VertexProcessor::setVertexShader<VS> (VertexProcessor.h:77-85): built-in VS id. */
-int swr_set_vertex_shader(swr_context* ctx, int vs_id);
+SWR_API int swr_set_vertex_shader(swr_context* ctx, int vs_id);
 /* VertexProcessor::setVertexAttribPointer (VertexProcessor.h:88, VertexProcessor.cpp:67-76).
  * `bytes` is the buffer size; the vertex count used for index bounds checks is
  * bytes / stride (the reference does not check indices). */
-int swr_set_vertex_attrib_pointer(swr_context* ctx, int index, int stride, const void* buffer,
+SWR_API int swr_set_vertex_attrib_pointer(swr_context* ctx, int index, int stride, const void* buffer,
                                   uint64_t bytes);
 /* VertexProcessor::drawElements (VertexProcessor.h:91, VertexProcessor.cpp:78-120).
  * indices: device uint32 array; values must be < 2^31 - 1 (the reference's int). */
-int swr_draw_elements(swr_context* ctx, int mode, uint64_t count, const uint32_t* indices,
+SWR_API int swr_draw_elements(swr_context* ctx, int mode, uint64_t count, const uint32_t* indices,
                       void* stream);
 
+/* Shader programs compiled in the caller's own nvcc translation unit: setVertexShader<VS>
+ * (VertexProcessor.h:77-85) and setPixelShader<PS> (Rasterizer.h:90-96) for shaders the
+ * library does not ship.  A program is the table of stage launchers that the header-only
+ * C++ front-end include/swr/Renderer.h instantiates for one VertexShaderBase- or
+ * PixelShaderBase-derived class (swr::program<Shader>()); the library borrows it, so it
+ * must outlive the draws that use it.  A program built against other headers (another
+ * layout of the structures it exchanges with the library) is rejected with SWR_EINVAL.
+ * The id-based setters and these replace each other. */
+typedef struct swr_program swr_program;
+SWR_API int swr_set_vertex_program(swr_context* ctx, const swr_program* program);
+SWR_API int swr_set_pixel_program(swr_context* ctx, const swr_program* program);
+
 /* Rasterizer::setRasterMode (Rasterizer.h:75-78). */
-int swr_set_raster_mode(swr_context* ctx, int mode);
+SWR_API int swr_set_raster_mode(swr_context* ctx, int mode);
 /* Rasterizer::setScissorRect (Rasterizer.h:81-87). */
-int swr_set_scissor_rect(swr_context* ctx, int x, int y, int width, int height);
+SWR_API int swr_set_scissor_rect(swr_context* ctx, int x, int y, int width, int height);
 /* Rasterizer::setPixelShader<PS> (Rasterizer.h:90-96): built-in PS id. */
-int swr_set_pixel_shader(swr_context* ctx, int ps_id);
+SWR_API int swr_set_pixel_shader(swr_context* ctx, int ps_id);
 /* Shader uniforms and render target (the reference's shader statics).  Copied. */
-int swr_set_uniforms(swr_context* ctx, const struct SwrUniforms* u);
+SWR_API int swr_set_uniforms(swr_context* ctx, const struct SwrUniforms* u);
 /* IRasterizer::draw{Point,Line,Triangle}List (IRasterizer.h:56-71, Rasterizer.h:116-141):
  * vertices are RasterizerVertex records (x, y, z, w, avar[16], pvar[16]; 36 floats) in
  * screen space; an index of -1 at the start of a primitive skips it. */
-int swr_draw_list(swr_context* ctx, int mode, const float* vertices, uint64_t nverts,
+SWR_API int swr_draw_list(swr_context* ctx, int mode, const float* vertices, uint64_t nverts,
                   const int32_t* indices, uint64_t count, void* stream);
 
 /* Batched rendering (no reference counterpart: the reference draws one mesh per
@@ -104,7 +125,7 @@ int swr_draw_list(swr_context* ctx, int mode, const float* vertices, uint64_t nv
  * batch is one pass of the pipeline (every kernel covers all items), so per-item results
  * equal separate swr_draw_elements calls. */
 typedef struct swr_draw_item {
-  int32_t vs_id, ps_id;
+  int32_t vs_id, ps_id;        /* built-in program ids; 0 = the context's current program */
   int32_t cull_mode, raster_mode;
   int32_t viewport[4];
   float depth_range[2];
@@ -119,16 +140,16 @@ typedef struct swr_draw_item {
   uint64_t prim_src_capacity;
 } swr_draw_item;
 
-int swr_draw_batch(swr_context* ctx, const swr_draw_item* items, int n, void* stream);
+SWR_API int swr_draw_batch(swr_context* ctx, const swr_draw_item* items, int n, void* stream);
 /* With graph mode on, swr_draw_batch captures its kernel sequence in a CUDA graph the first
  * time a batch layout (item count, sizes, shaders, modes) is seen and replays it for later
  * batches with the same layout; uniforms and buffer pointers are refreshed on every call.
  * Triangle swr_draw_elements calls then run as one-item batches (so they replay too),
  * except while profiling is on (stage events need the launch-by-launch path). */
-int swr_set_graph_mode(swr_context* ctx, int on);
+SWR_API int swr_set_graph_mode(swr_context* ctx, int on);
 
 /* Wait for the stream, report and reset the accumulated status. */
-int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
+SWR_API int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
 /* Queue sizes (no reference counterpart: the reference grows std::vectors).  A context
  * sizes its primitive queue (triangles after clipping and culling) and its bin-entry queue
  * ((tile, primitive) pairs) ahead of every draw from the submitted count; a draw that
@@ -137,25 +158,25 @@ int swr_finish(swr_context* ctx, void* stream, swr_stats* stats);
  * swr_set_queue_capacity fixes either size instead (0 keeps the automatic sizing): a
  * caller that knows its scenes (an autotuned batch) pre-sizes the queues once; they are
  * still grown after an overflow.  swr_get_queue_capacity reports the current sizes. */
-int swr_set_queue_capacity(swr_context* ctx, uint64_t primitives, uint64_t bin_entries);
-int swr_get_queue_capacity(swr_context* ctx, uint64_t* primitives, uint64_t* bin_entries);
+SWR_API int swr_set_queue_capacity(swr_context* ctx, uint64_t primitives, uint64_t bin_entries);
+SWR_API int swr_get_queue_capacity(swr_context* ctx, uint64_t* primitives, uint64_t* bin_entries);
 /* Device-memory budget (no reference counterpart): the context's scratch allocations
  * fail with SWR_ENOMEM, queuing nothing, once they would hold more than `bytes` (0: no
  * limit, the default), exactly as when cudaMalloc itself fails; swr_memory_used reports
  * the bytes held. */
-int swr_set_memory_limit(swr_context* ctx, uint64_t bytes);
-int swr_memory_used(swr_context* ctx, uint64_t* bytes);
+SWR_API int swr_set_memory_limit(swr_context* ctx, uint64_t bytes);
+SWR_API int swr_memory_used(swr_context* ctx, uint64_t* bytes);
 /* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels. */
-int swr_set_tile_size(swr_context* ctx, int tile);
-const char* swr_status_string(int status);
+SWR_API int swr_set_tile_size(swr_context* ctx, int tile);
+SWR_API const char* swr_status_string(int status);
 
 /* Tracing (no reference counterpart; the reference has only Benchmark.cpp's chrono).
  * With profiling on, every draw records CUDA events at its stage boundaries on its own
  * stream; swr_stage_times waits for the draws recorded since its previous call and returns
  * their summed durations in ms for 5 stages: vertex shading, clip/cull/assembly, triangle
  * setup, binning, tile raster. */
-int swr_set_profiling(swr_context* ctx, int on);
-int swr_stage_times(swr_context* ctx, float* ms5);
+SWR_API int swr_set_profiling(swr_context* ctx, int on);
+SWR_API int swr_stage_times(swr_context* ctx, float* ms5);
 
 /* Primitive sources (no reference counterpart; needed by swr_backward).  While set, each
  * triangle swr_draw_elements call writes out[k] = t, the source triangle (indices
@@ -165,7 +186,7 @@ int swr_stage_times(swr_context* ctx, float* ms5);
  * yields several primitives with one source.  At most `capacity` entries are written; a
  * draw with more primitives makes swr_finish return SWR_EINVAL.  NULL turns it off.
  * (swr_draw_item.prim_src is the same output for one item of a batch.) */
-int swr_set_primitive_source(swr_context* ctx, int32_t* out, uint64_t capacity);
+SWR_API int swr_set_primitive_source(swr_context* ctx, int32_t* out, uint64_t capacity);
 
 /* Differentiable rendering (no reference counterpart: the reference renders forward only).
  * The forward is an ordinary draw with vertex shader SWR_VS_POS_RGB_UV and pixel shader
@@ -205,7 +226,7 @@ typedef struct swr_backward_args {
  * first).  Ids beyond nprims / the triangle count / the vertex count are skipped and make
  * swr_finish return SWR_EINDEX.  Float atomics make the summation order (not the terms)
  * vary from run to run. */
-int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad_view* views, int nviews,
+SWR_API int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad_view* views, int nviews,
                  void* stream);
 
 /* Mip-mapped texturing (the reference's example texture, src/examples/Texture.h, used by
@@ -217,8 +238,8 @@ int swr_backward(swr_context* ctx, const swr_backward_args* args, const swr_grad
  * swr_mip_chain_size gives the level count and the total texels of the chain;
  * swr_build_mip_chain fills it from a level-0 image (Texture::generateMipmaps,
  * Texture.h:220-293; 2 x 2 box filter).  Both buffers are device memory. */
-int swr_mip_chain_size(int width, int height, int* levels, uint64_t* texels);
-int swr_build_mip_chain(const uint32_t* base, int width, int height, uint32_t* chain, void* stream);
+SWR_API int swr_mip_chain_size(int width, int height, int* levels, uint64_t* texels);
+SWR_API int swr_build_mip_chain(const uint32_t* base, int width, int height, uint32_t* chain, void* stream);
 
 /* OBJ ingestion: ObjData::loadFromFile + ObjData::toVertexArray of the reference's
  * examples (src/examples/ObjData.cpp:46-199).  A mesh holds the deduplicated vertex array
@@ -229,19 +250,19 @@ int swr_build_mip_chain(const uint32_t* base, int width, int height, uint32_t* c
  * host memory (no GPU needed); swr_obj_upload copies them to device buffers on `stream` and
  * waits for it.  Either array pointer may be NULL. */
 typedef struct swr_obj_mesh swr_obj_mesh;
-int swr_obj_parse(const char* text, uint64_t len, swr_obj_mesh** out);
-int swr_obj_load(const char* path, swr_obj_mesh** out);
-int swr_obj_counts(const swr_obj_mesh* mesh, uint64_t* nverts, uint64_t* nindices);
-int swr_obj_read(const swr_obj_mesh* mesh, float* vdata, int32_t* idata);
-int swr_obj_upload(const swr_obj_mesh* mesh, float* vdata, int32_t* idata, void* stream);
-int swr_obj_free(swr_obj_mesh* mesh);
+SWR_API int swr_obj_parse(const char* text, uint64_t len, swr_obj_mesh** out);
+SWR_API int swr_obj_load(const char* path, swr_obj_mesh** out);
+SWR_API int swr_obj_counts(const swr_obj_mesh* mesh, uint64_t* nverts, uint64_t* nindices);
+SWR_API int swr_obj_read(const swr_obj_mesh* mesh, float* vdata, int32_t* idata);
+SWR_API int swr_obj_upload(const swr_obj_mesh* mesh, float* vdata, int32_t* idata, void* stream);
+SWR_API int swr_obj_free(swr_obj_mesh* mesh);
 
 /* Render-target clear (no reference counterpart: its applications clear their own
  * buffers, e.g. Box.cpp's SDL_FillRect): fills the target named by u -- colour
  * (color_bytes = 4 or 16 per pixel, the pattern at clear_color), depth (clear_depth) and,
  * when present, frag_count (0) and winner (-1) -- in one kernel on `stream`.  Buffers must
  * be 16-byte aligned (cudaMalloc is). */
-int swr_clear_target(const struct SwrUniforms* u, int color_bytes, const void* clear_color, float clear_depth,
+SWR_API int swr_clear_target(const struct SwrUniforms* u, int color_bytes, const void* clear_color, float clear_depth,
                      void* stream);
 
 /* Headless presentation (replaces the SDL window surface of the reference's examples,
@@ -250,7 +271,7 @@ int swr_clear_target(const struct SwrUniforms* u, int color_bytes, const void* c
 #define SWR_PIXELS_RGBA8 0    /* uint32 per pixel, R in bits 0-7 (the RGBA8 built-in shaders) */
 #define SWR_PIXELS_XRGB8 1    /* uint32 0x00RRGGBB (SWR_PS_TEX_MIP, the SDL surface format) */
 #define SWR_PIXELS_RGBA32F 2  /* 4 floats per pixel, clamped to [0, 1] and rounded */
-int swr_write_image(const char* path, const void* pixels, int width, int height, int format);
+SWR_API int swr_write_image(const char* path, const void* pixels, int width, int height, int format);
 
 /* Allocation-free triangle-list draw.  No counterpart in the reference (whose CPU
  * rasterizer needs no device scratch).  It is swr_draw_list(SWR_DRAW_TRIANGLE, ...) for
@@ -269,7 +290,7 @@ int swr_write_image(const char* path, const void* pixels, int width, int height,
  * can allocate -- make it once at start-up, before any stream capture.  After
  * cudaDeviceReset the next call repeats the set-up in the new context.  All calls share
  * the array: calls that overlap on the GPU race, so serialise them. */
-int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int ps_id, int raster_mode,
+SWR_API int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int ps_id, int raster_mode,
                                    int scissor_x, int scissor_y, int scissor_w, int scissor_h,
                                    const float* vertices, uint64_t nverts,
                                    const int32_t* indices, uint64_t count, void* stream,

@@ -18,8 +18,11 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libswr_gb300.so")
 SOURCES = ["swr_core.cu", "swr_vs.cu", "swr_ps.cu", "swr_ps_lambert.cu", "swr_ps_color.cu", "swr_ps_tex.cu", "swr_ps_deriv.cu", "swr_capi.cu", "swr_noalloc.cu", "swr_backward.cu", "swr_texture.cu", "swr_obj.cpp", "swr_image.cpp", "swr_target.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Hidden visibility: only the C ABI (SWR_API in include/swr_gb300.h) is exported, so kernel
+# templates a caller instantiates for its own shaders never interpose on the library's.
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
-         "-ftz=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+         "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
+         "-Xptxas", "-warn-spills"]
 
 
 def nvcc():

@@ -102,11 +102,13 @@ struct swr_context {
   float dn = 0.0f, df = 1.0f;
   int cull = SWR_CULL_CW;
   int vs_id = 0;
+  const swr::VsOps* vs_cur = nullptr;  // set by swr_set_vertex_shader or swr_set_vertex_program
   swr::Attrib attribs[8];
   // Rasterizer state
   int raster_mode = SWR_RASTER_SPAN;
   int sc_x = 0, sc_y = 0, sc_w = 0, sc_h = 0;
   int ps_id = 0;
+  const swr::PsOps* ps_cur = nullptr;  // set by swr_set_pixel_shader or swr_set_pixel_program
   SwrUniforms u;
   bool have_u = false;
   int tile = 16;
@@ -540,6 +542,34 @@ int swr_set_cull_mode(swr_context* c, int mode) {
 int swr_set_vertex_shader(swr_context* c, int id) {
   if (!c || !vs_ops(id)) return SWR_EINVAL;
   c->vs_id = id;
+  c->vs_cur = vs_ops(id);
+  return SWR_OK;
+}
+
+static bool program_ok(const swr_program* p, uint32_t kind) {
+  if (!p || p->magic != SWR_PROGRAM_MAGIC || p->abi != SWR_PROGRAM_ABI || p->kind != kind) return false;
+  uint32_t mine[10];
+  swr_program_layout(mine);
+  for (int i = 0; i < 10; ++i)
+    if (p->sizes[i] != mine[i]) return false;
+  return kind == SWR_PROGRAM_VERTEX ? p->vs != nullptr : p->ps != nullptr;
+}
+
+int swr_set_vertex_program(swr_context* c, const swr_program* p) {
+  if (!c || !program_ok(p, SWR_PROGRAM_VERTEX)) return SWR_EINVAL;
+  const VsOps* o = p->vs;
+  if (o->attribs < 0 || o->attribs > 8 || o->A < 0 || o->A > 16 || o->P < 0 || o->P > 16) return SWR_EINVAL;
+  c->vs_id = 0;
+  c->vs_cur = o;
+  return SWR_OK;
+}
+
+int swr_set_pixel_program(swr_context* c, const swr_program* p) {
+  if (!c || !program_ok(p, SWR_PROGRAM_PIXEL)) return SWR_EINVAL;
+  const PsOps* o = p->ps;
+  if (o->A < 0 || o->A > 16 || o->P < 0 || o->P > 16) return SWR_EINVAL;
+  c->ps_id = 0;
+  c->ps_cur = o;
   return SWR_OK;
 }
 
@@ -566,6 +596,7 @@ int swr_set_scissor_rect(swr_context* c, int x, int y, int w, int h) {
 int swr_set_pixel_shader(swr_context* c, int id) {
   if (!c || !ps_ops(id)) return SWR_EINVAL;
   c->ps_id = id;
+  c->ps_cur = ps_ops(id);
   return SWR_OK;
 }
 
@@ -619,8 +650,8 @@ int swr_set_tile_size(swr_context* c, int tile) {
 
 int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* indices, void* stream) {
   if (!c || !c->have_u) return SWR_EINVAL;
-  const VsOps* vs = vs_ops(c->vs_id);
-  const PsOps* ps = ps_ops(c->ps_id);
+  const VsOps* vs = c->vs_cur;
+  const PsOps* ps = c->ps_cur;
   if (!vs || !ps) return SWR_EINVAL;
   if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
   if (ps->needs_eq && mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // PixelData::equations is null
@@ -628,8 +659,8 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
     // graph mode: the draw is a one-item batch, captured once per layout and replayed
     swr_draw_item it;
     memset(&it, 0, sizeof(it));
-    it.vs_id = c->vs_id;
-    it.ps_id = c->ps_id;
+    it.vs_id = 0;  // the context's current programs
+    it.ps_id = 0;
     it.cull_mode = c->cull;
     it.raster_mode = c->raster_mode;
     it.viewport[0] = c->vp_x; it.viewport[1] = c->vp_y; it.viewport[2] = c->vp_w; it.viewport[3] = c->vp_h;
@@ -654,8 +685,9 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   uint64_t nverts = ~0ull;
   for (int a = 0; a < vs->attribs; ++a) {
     const Attrib& at = c->attribs[a];
-    const uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
     if (!at.ptr || at.stride <= 0 || at.bytes == 0) return SWR_EINVAL;
+    uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
+    if (!elem) elem = (uint64_t)at.stride;
     // element i occupies [i * stride, i * stride + elem): the last one must fit
     const uint64_t n = at.bytes >= elem ? (at.bytes - elem) / (uint64_t)at.stride + 1 : 0;
     nverts = n < nverts ? n : nverts;
@@ -717,7 +749,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
 int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nverts, const int32_t* indices,
                   uint64_t count, void* stream) {
   if (!c || !c->have_u) return SWR_EINVAL;
-  const PsOps* ps = ps_ops(c->ps_id);
+  const PsOps* ps = c->ps_cur;
   if (!ps) return SWR_EINVAL;
   if (mode < SWR_DRAW_POINT || mode > SWR_DRAW_TRIANGLE) return SWR_EINVAL;
   if (ps->needs_eq && mode != SWR_DRAW_TRIANGLE) return SWR_EINVAL;  // PixelData::equations is null
@@ -765,8 +797,9 @@ int swr_set_graph_mode(swr_context* c, int on) {
 
 int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stream) {
   if (!c || !items || n <= 0) return SWR_EINVAL;
-  const VsOps* vs = vs_ops(items[0].vs_id);
-  const PsOps* ps = ps_ops(items[0].ps_id);
+  // id 0: the context's current program (a built-in one or a caller's swr_program)
+  const VsOps* vs = items[0].vs_id ? vs_ops(items[0].vs_id) : c->vs_cur;
+  const PsOps* ps = items[0].ps_id ? ps_ops(items[0].ps_id) : c->ps_cur;
   if (!vs || !ps) return SWR_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   std::vector<SwrDrawDesc> D(n);
@@ -786,8 +819,9 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     if (u.width <= 0 || u.height <= 0 || !u.color) return SWR_EINVAL;
     uint64_t nv = ~0ull;
     for (int a = 0; a < vs->attribs; ++a) {
-      const uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
       if (!it.attrib[a] || it.attrib_stride[a] <= 0 || it.attrib_bytes[a] == 0) return SWR_EINVAL;
+      uint64_t elem = (uint64_t)vs->elem_bytes[a < 2 ? a : 1];
+      if (!elem) elem = (uint64_t)it.attrib_stride[a];
       const uint64_t k = it.attrib_bytes[a] >= elem ? (it.attrib_bytes[a] - elem) / (uint64_t)it.attrib_stride[a] + 1 : 0;
       nv = k < nv ? k : nv;
     }
@@ -888,6 +922,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   memcpy(h + o_vb, vbase.data(), 4 * n);
   memcpy(h + o_bb, bbase.data(), 4 * n);
   memcpy(h + o_tb, tbase.data(), 4 * ntg);
+  mix((uint64_t)(uintptr_t)vs); mix((uint64_t)(uintptr_t)ps);  // the programs (their kernels)
   mix((uint64_t)vs->S); mix((uint64_t)ps->R); mix((uint64_t)c->tile); mix((uint64_t)n);
   mix(c->cap_prims); mix(c->cap_pairs); mix(c->cap_clip_slots); mix(c->cap_clip_verts);
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,

@@ -8,7 +8,8 @@ namespace swr {
 
 struct VsOps {
   int attribs, A, P, S;  // AttribCount, AVarCount, PVarCount, post-transform record stride
-  int elem_bytes[2];     // bytes read per element of attribute streams 0 and 1
+  int elem_bytes[2];     // bytes read per element of attribute streams 0 and 1 (0: one whole stride,
+                         // for every stream)
   void (*vertex)(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase, uint32_t nverts,
                  float* ptv, cudaStream_t s);
   void (*assemble_count)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
@@ -43,3 +44,36 @@ const VsOps* vs_ops(int id);
 const PsOps* ps_ops(int id);
 
 }  // namespace swr
+
+// A shader program compiled in a caller's own translation unit (include/swr/Renderer.h):
+// the stage-launcher table of one vertex or pixel shader, handed to the library through
+// swr_set_vertex_program / swr_set_pixel_program.  The kernels it launches are built from
+// these headers in the caller's unit, so the library checks that both sides agree on the
+// layout of every structure that crosses between them.
+#define SWR_PROGRAM_MAGIC 0x50525753u  // "SWRP"
+#define SWR_PROGRAM_ABI 1u             // bumped with any change to VsOps, PsOps or their argument structs
+#define SWR_PROGRAM_VERTEX 1u
+#define SWR_PROGRAM_PIXEL 2u
+
+struct swr_program {
+  uint32_t magic;     // SWR_PROGRAM_MAGIC
+  uint32_t abi;       // SWR_PROGRAM_ABI
+  uint32_t kind;      // SWR_PROGRAM_VERTEX or SWR_PROGRAM_PIXEL
+  uint32_t sizes[10]; // swr_program_layout()
+  const swr::VsOps* vs;
+  const swr::PsOps* ps;
+};
+
+// Sizes of the structures the launchers exchange with the library.
+inline void swr_program_layout(uint32_t* s) {
+  s[0] = (uint32_t)sizeof(swr::VsOps);
+  s[1] = (uint32_t)sizeof(swr::PsOps);
+  s[2] = (uint32_t)sizeof(SwrDrawDesc);
+  s[3] = (uint32_t)sizeof(SwrTargetDesc);
+  s[4] = (uint32_t)sizeof(swr::AssembleArgs);
+  s[5] = (uint32_t)sizeof(swr::SetupArgs);
+  s[6] = (uint32_t)sizeof(swr::RasterArgs);
+  s[7] = (uint32_t)sizeof(swr::LpFragArgs);
+  s[8] = (uint32_t)sizeof(swr::LpShadeArgs);
+  s[9] = (uint32_t)sizeof(SwrUniforms);
+}

@@ -708,6 +708,18 @@ struct SwrRasterOccupancy<PS, decltype((void)PS::RasterOccupancy)> {
   enum { value = PS::RasterOccupancy };
 };
 
+// Pixel shaders whose drawPixel has side effects beyond its State (user shaders that write
+// their own buffers, include/swr/Renderer.h): the rasterizer must call drawPixel once per
+// fragment in primitive order and may not evaluate anything of the shader ahead of it.
+template <class PS, class = void>
+struct SwrNoCompact {
+  enum { value = 0 };
+};
+template <class PS>
+struct SwrNoCompact<PS, decltype((void)PS::NoCompact)> {
+  enum { value = PS::NoCompact };
+};
+
 // Pixel shaders whose shade() reads the triangle's equations (PixelData::equations) --
 // set only for triangles; the reference dereferences a null pointer for points and lines.
 template <class PS, class = void>

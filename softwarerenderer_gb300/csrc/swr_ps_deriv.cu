@@ -4,8 +4,8 @@
 namespace swr {
 
 const PsOps* ps_ops_deriv(int id) {
-  static const PsOps kPsDiff = make<PsDiff>();
-  static const PsOps kPsPerspDeriv = make<PsPerspDeriv>();
+  static const PsOps kPsDiff = make_ps<PsDiff>();
+  static const PsOps kPsPerspDeriv = make_ps<PsPerspDeriv>();
   switch (id) {
     case SWR_PS_DIFF: return &kPsDiff;
     case SWR_PS_PERSP_DERIV: return &kPsPerspDeriv;

@@ -77,7 +77,7 @@ void run_lp_shade(const LpShadeArgs& a, cudaStream_t s) {
 }
 
 template <class PS>
-PsOps make() {
+PsOps make_ps() {
   PsOps o;
   o.A = PS::AVarCount;
   o.P = PS::PVarCount;

@@ -4,8 +4,8 @@
 namespace swr {
 
 const PsOps* ps_ops_tex(int id) {
-  static const PsOps kPsTexNearest = make<PsTexNearest>();
-  static const PsOps kPsTexMip = make<PsTexMip>();
+  static const PsOps kPsTexNearest = make_ps<PsTexNearest>();
+  static const PsOps kPsTexMip = make_ps<PsTexMip>();
   switch (id) {
     case SWR_PS_TEX_NEAREST: return &kPsTexNearest;
     case SWR_PS_TEX_MIP: return &kPsTexMip;

@@ -1188,7 +1188,8 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   constexpr int PPT = TILE * TILE / 256;  // pixels per thread
   constexpr int NBX = TILE / SWR_BLOCK;   // blocks per tile row
   constexpr int NB = NBX * NBX;
-  constexpr int FB = sizeof(Color) > 4 ? 512 : 1024;  // compacted fragments per chunk
+  constexpr bool kCompact = !SwrNoCompact<PS>::value;
+  constexpr int FB = !kCompact ? 32 : (sizeof(Color) > 4 ? 512 : 1024);  // compacted fragments per chunk
   constexpr int SMALL = 64;
   __shared__ float4 srec4[CH * RL::R / 4];
   float* srec = (float*)srec4;
@@ -1525,7 +1526,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         for (int w = 0; w < NW; ++w) {
           cnt[w] = w ? sex[w * 32 + lane] : cnt0;
           cul[w] = w ? scomp[w * 32 + lane] != 0 : cul0;
-          cand[w] = cnt[w] <= SMALL && !cul[w] && !deep ? cnt[w] : 0u;
+          cand[w] = kCompact && cnt[w] <= SMALL && !cul[w] && !deep ? cnt[w] : 0u;
           inc[w] = cand[w];
         }
 #pragma unroll
@@ -1541,7 +1542,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         for (int w = 0; w < NW; ++w) {
           const uint32_t ex = carry + inc[w] - cand[w];
           carry += __shfl_sync(0xffffffffu, inc[w], 31);
-          const bool comp = !cul[w] && !deep && cnt[w] <= SMALL && ex + cnt[w] <= FB;
+          const bool comp = kCompact && !cul[w] && !deep && cnt[w] <= SMALL && ex + cnt[w] <= FB;
           if (w * 32 + lane < n) {
             sex[w * 32 + lane] = ex;
             scomp[w * 32 + lane] = comp ? 1 : 0;

@@ -1,61 +1,14 @@
 // Vertex-stage kernels of the built-in vertex shaders.
-#include "swr_ops.h"
+#include "swr_vs_impl.cuh"
 
 namespace swr {
 namespace {
 
-constexpr int kGrid = 152 * 8;
-
-template <class VS>
-void run_vertex(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase, uint32_t nverts,
-                float* ptv, cudaStream_t s) {
-  if (!nverts) return;
-  const uint32_t want = (nverts + 255) / 256;
-  const int grid = (int)(want < (uint32_t)kGrid ? want : (uint32_t)kGrid);
-  k_vertex<VS><<<grid, 256, 0, s>>>(draws, ndraws, draw_vbase, nverts, ptv);
-}
-
-template <class VS>
-void run_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_count<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
-}
-
-template <class VS>
-void run_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
-}
-
-template <class VS>
-void run_lp_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_lp_count<VS::AVarCount, VS::PVarCount><<<nbatches, 256, 0, s>>>(a);
-}
-
-void run_lp_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_lp_emit<<<nbatches, 256, 0, s>>>(a);
-}
-
-template <class VS>
-VsOps make() {
-  VsOps o;
-  o.attribs = VS::AttribCount;
-  o.A = VS::AVarCount;
-  o.P = VS::PVarCount;
-  o.S = VLayout<VS::AVarCount, VS::PVarCount>::S;
-  o.elem_bytes[0] = VS::Bytes0;
-  o.elem_bytes[1] = VS::Bytes1;
-  o.vertex = &run_vertex<VS>;
-  o.assemble_count = &run_count<VS>;
-  o.assemble_emit = &run_emit<VS>;
-  o.assemble_lp_count = &run_lp_count<VS>;
-  o.assemble_lp_emit = &run_lp_emit;
-  return o;
-}
-
-const VsOps kPosUV = make<VsPosUV>();
-const VsOps kPosNrmUV = make<VsPosNrmUV>();
-const VsOps kPosRGB = make<VsPosRGB>();
-const VsOps kPosRGBAffine = make<VsPosRGBAffine>();
-const VsOps kPosRGBUV = make<VsPosRGBUV>();
+const VsOps kPosUV = make_vs<VsPosUV>();
+const VsOps kPosNrmUV = make_vs<VsPosNrmUV>();
+const VsOps kPosRGB = make_vs<VsPosRGB>();
+const VsOps kPosRGBAffine = make_vs<VsPosRGBAffine>();
+const VsOps kPosRGBUV = make_vs<VsPosRGBUV>();
 
 }  // namespace
 

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     txt = open(os.path.join(ROOT, "include", "swr_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(swr_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:SWR_API\s+)?(?:int|const char\*)\s+(swr_\w+)\s*\(", txt, re.M)))
 
 
 def test_header_declares_the_reference_api():
