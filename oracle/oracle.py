@@ -96,6 +96,15 @@ def load(which="port"):
             lib.oracle_ref_obj.restype = ctypes.c_int
             lib.oracle_ref_random.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p]
             lib.oracle_ref_random.restype = None
+        if hasattr(lib, "oracle_tex_sample"):
+            lib.oracle_tex_sample.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+            lib.oracle_tex_sample.restype = None
+        if hasattr(lib, "oracle_ref_tex_sample"):
+            lib.oracle_ref_tex_sample.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                  ctypes.c_void_p]
+            lib.oracle_ref_tex_sample.restype = ctypes.c_int
         if hasattr(lib, "oracle_log2"):
             lib.oracle_log2.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
             lib.oracle_log2.restype = None
@@ -104,6 +113,14 @@ def load(which="port"):
             lib.oracle_fold_selftest.restype = ctypes.c_uint64
         _LIBS[which] = Oracle(lib, which)
     return _LIBS[which]
+
+
+def scenes_chain_size(w, h):
+    n = w * h
+    while w > 1 or h > 1:
+        w, h = max(1, w // 2), max(1, h // 2)
+        n += w * h
+    return n
 
 
 def _ptr(a):
@@ -132,6 +149,30 @@ class Oracle:
         """n values of the reference examples' Random(seed).NextDouble() (ref library only)."""
         out = np.zeros(n, np.float64)
         self.lib.oracle_ref_random(int(seed), int(n), out.ctypes.data)
+        return out
+
+    def tex_sample(self, texture, q, max_aniso=0):
+        """Sampled 0x00RRGGBB colours for records q (n x 6: u, v, dudx, dvdx, dudy, dvdy) of a
+        w x h texture.  The port samples the mip chain `texture` with swr_tex_sample
+        (texture = scenes.mip_chain of the level-0 image); the reference builds its own chain
+        from the level-0 image and samples it with Texture::sample, and then also returns
+        that chain."""
+        q = np.ascontiguousarray(q, np.float32)
+        out = np.zeros(q.shape[0], np.uint32)
+        h, w = texture.shape[:2] if texture.ndim == 2 else (None, None)
+        if self.which == "ref":
+            base = np.ascontiguousarray(texture, np.uint32)
+            chain = np.zeros(scenes_chain_size(w, h), np.uint32)
+            self.lib.oracle_ref_tex_sample(base.ctypes.data, w, h, max_aniso, q.ctypes.data, out.ctypes.data,
+                                           q.shape[0], chain.ctypes.data)
+            return out, chain
+        raise TypeError("the port samples a chain: use tex_sample_chain")
+
+    def tex_sample_chain(self, chain, w, h, q, max_aniso=0):
+        q = np.ascontiguousarray(q, np.float32)
+        chain = np.ascontiguousarray(chain, np.uint32)
+        out = np.zeros(q.shape[0], np.uint32)
+        self.lib.oracle_tex_sample(chain.ctypes.data, w, h, max_aniso, q.ctypes.data, out.ctypes.data, q.shape[0])
         return out
 
     def log2(self, x):

@@ -8,6 +8,7 @@
 // Every floating-point expression keeps the reference's operation order; build with
 // -ffp-contract=off (no FMA) so each operation rounds exactly once.
 // OpenMP pragmas sit where the reference has them (Rasterizer.h:257, :369, :396).
+#include <omp.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -258,8 +259,7 @@ struct Raster {
     const int stepsX = (bx1 - bx0) / kBlock + 1;
     const int stepsY = (by1 - by0) / kBlock + 1;
     uint64_t frags = 0, outside = 0;
-#pragma omp parallel for reduction(+ : frags, outside)
-    for (int i = 0; i < stepsX * stepsY; ++i) {
+    auto blk = [&](int i, uint64_t& frags, uint64_t& outside) {
       const int sx = i % stepsX, sy = i / stepsX;
       const int x = bx0 + sx * kBlock, y = by0 + sy * kBlock;
       const float xf = x + 0.5f, yf = y + 0.5f;
@@ -282,6 +282,14 @@ struct Raster {
       } else {
         block<true>(e, x, y, prim, frags, outside);
       }
+    };
+    // The reference's OpenMP loop over blocks (Rasterizer.h:257); a one-thread run skips
+    // the team fork per triangle, as the reference built without OpenMP does.
+    if (omp_get_max_threads() > 1) {
+#pragma omp parallel for reduction(+ : frags, outside)
+      for (int i = 0; i < stepsX * stepsY; ++i) blk(i, frags, outside);
+    } else {
+      for (int i = 0; i < stepsX * stepsY; ++i) blk(i, frags, outside);
     }
     cnt->frags += frags;
     cnt->outside += outside;
@@ -293,14 +301,19 @@ struct Raster {
     const float is2 = (v2.x - v0.x) / (v2.y - v0.y);
     uint64_t frags = 0, outside = 0;
     const int y0 = int(v0.y + 0.5f), y1 = int(v1.y + 0.5f);
-#pragma omp parallel for reduction(+ : frags, outside)
-    for (int y = y0; y < y1; y++) {
+    auto row = [&](int y, uint64_t& frags, uint64_t& outside) {
       const float dy = (y - v0.y) + 0.5f;
       const float cx1 = v0.x + is1 * dy + 0.5f;
       const float cx2 = v0.x + is2 * dy + 0.5f;
       const int xl = swr_maxi(minX, (int)cx1);
       const int xr = swr_mini(maxX, (int)cx2);
       span(e, xl, y, xr, prim, frags, outside);
+    };
+    if (omp_get_max_threads() > 1) {  // OpenMP over scanlines (Rasterizer.h:369)
+#pragma omp parallel for reduction(+ : frags, outside)
+      for (int y = y0; y < y1; y++) row(y, frags, outside);
+    } else {
+      for (int y = y0; y < y1; y++) row(y, frags, outside);
     }
     cnt->frags += frags;
     cnt->outside += outside;
@@ -312,14 +325,19 @@ struct Raster {
     const float is2 = (v2.x - v1.x) / (v2.y - v1.y);
     uint64_t frags = 0, outside = 0;
     const int ytop = int(v2.y - 0.5f), yend = int(v0.y - 0.5f);
-#pragma omp parallel for reduction(+ : frags, outside)
-    for (int y = ytop; y > yend; y--) {
+    auto row = [&](int y, uint64_t& frags, uint64_t& outside) {
       const float dy = (y - v2.y) + 0.5f;
       const float cx1 = v2.x + is1 * dy + 0.5f;
       const float cx2 = v2.x + is2 * dy + 0.5f;
       const int xl = swr_maxi(minX, (int)cx1);
       const int xr = swr_mini(maxX, (int)cx2);
       span(e, xl, y, xr, prim, frags, outside);
+    };
+    if (omp_get_max_threads() > 1) {  // OpenMP over scanlines (Rasterizer.h:396)
+#pragma omp parallel for reduction(+ : frags, outside)
+      for (int y = ytop; y > yend; y--) row(y, frags, outside);
+    } else {
+      for (int y = ytop; y > yend; y--) row(y, frags, outside);
     }
     cnt->frags += frags;
     cnt->outside += outside;
@@ -729,6 +747,22 @@ extern "C" float oracle_fold(float v, float a, int k) { return swr_fold(v, a, k)
 // swr_log2 and the mip-mapped sampler exposed for the tests of the texture subsystem.
 extern "C" void oracle_log2(const float* x, float* out, uint64_t n) {
   for (uint64_t i = 0; i < n; ++i) out[i] = swr_log2(x[i]);
+}
+
+// swr_tex_sample (the sampler the GPU shader PsTexMip runs) over a mip chain of a w x h
+// texture: q holds n records {u, v, dudx, dvdx, dudy, dvdy}.
+extern "C" void oracle_tex_sample(const uint32_t* chain, int w, int h, int max_aniso, const float* q, uint32_t* out,
+                                  uint64_t n) {
+  SwrUniforms u;
+  memset(&u, 0, sizeof(u));
+  u.tex = chain;
+  u.tex_w = w;
+  u.tex_h = h;
+  u.max_aniso = max_aniso;
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* r = q + 6 * i;
+    out[i] = swr_tex_sample(u, r[0], r[1], r[2], r[3], r[4], r[5]);
+  }
 }
 
 // Randomized check of swr_fold against plain serial stepping: returns the number of

@@ -1,8 +1,9 @@
 """Generate tests/golden/golden.json by running the reference library itself.
 
-The reference's own sources (src/renderer of trenki2/SoftwareRenderer) are compiled
-unmodified with oracle/ref_harness.cpp (make -C oracle ref; needs the reference checkout,
-REFERENCE=/path/to/SoftwareRenderer).  For every scene spec below the harness renders the
+The reference's own sources (src/renderer of trenki2/SoftwareRenderer, and for the Box
+example's frames the mip-mapped sampler of src/examples/Texture.h) are compiled unmodified
+with oracle/ref_harness.cpp (make -C oracle ref; needs the reference checkout named by
+SWR_REFERENCE).  For every scene spec below the harness renders the
 seeded scene and the fixture records the reference's counters and a SHA-256 of each
 buffer the pixel shader writes (colour, depth, per-pixel drawPixel count, winning
 primitive).  Scenes are rebuilt from their specs by softwarerenderer_gb300.scenes, which is
@@ -59,7 +60,8 @@ def main():
         res.append({"spec": sp, "name": sc.name, "inputs": scenes.scene_digest(sc), "stats": {k: int(st[k]) for k in ("fragments", "outside", "primitives")},
                     "sha256": digest(tg.arrays())})
     with open(OUT, "w") as f:
-        json.dump({"generator": "reference library (src/renderer) via oracle/ref_harness.cpp",
+        json.dump({"generator": "reference library (src/renderer; Box frames: src/examples/Texture.h) via "
+                                "oracle/ref_harness.cpp",
                    "cases": res}, f, indent=0)
     print(f"{len(res)} cases in {time.time() - t0:.1f} s -> {OUT}")
 

@@ -58,3 +58,42 @@ def test_derivative_shaders_reject_points_and_lines(port, mode):
     sc.indices = sc.indices[:len(sc.indices) // 6 * 6]
     with pytest.raises(ValueError):
         port.draw(sc, scenes.Target(sc))
+
+
+def _ref_or_skip():
+    import os
+    from oracle import oracle
+    if not os.path.exists(oracle.PATHS["ref"]):
+        pytest.skip("reference library not built (needs the reference checkout, SWR_REFERENCE)")
+    return oracle.load("ref")
+
+
+def _footprints(rng, n):
+    """Texture coordinates across several wraps and pixel footprints from far below one
+    texel to far above the whole texture, isotropic to strongly anisotropic, any sign."""
+    q = np.empty((n, 6), np.float32)
+    q[:, 0:2] = rng.uniform(-3.0, 3.0, (n, 2))
+    mag = np.exp2(rng.uniform(-16.0, 2.0, (n, 4))) * rng.choice([-1.0, 1.0], (n, 4))
+    squash = rng.random(n) < 0.3  # one axis far shorter than the other
+    mag[squash, 2:4] *= np.exp2(rng.uniform(-8.0, 0.0, (int(squash.sum()), 1)))
+    zero = rng.random((n, 4)) < 0.02
+    mag[zero] = 0.0
+    q[:, 2:6] = mag
+    return q
+
+
+@pytest.mark.parametrize("w,h,aniso", [(256, 256, 0), (512, 128, 16), (37, 5, 3), (64, 64, 1), (1, 32, 0)])
+def test_sampler_matches_reference_texture(port, w, h, aniso):
+    """swr_tex_sample (the GPU shader's sampler) against the reference's own Texture::sample
+    and Texture::generateMipmaps (src/examples/Texture.h:35-293, compiled unmodified over
+    memory surfaces): the mip chain and every sampled colour bit for bit."""
+    ref = _ref_or_skip()
+    rng = np.random.default_rng(w * 7 + h)
+    tex = scenes.rgb_texture(w, h, seed=w + h)
+    q = _footprints(rng, 200_000)
+    want, ref_chain = ref.tex_sample(tex, q, max_aniso=aniso)
+    chain = scenes.mip_chain(tex)
+    assert np.array_equal(chain, ref_chain)
+    got = port.tex_sample_chain(chain, w, h, q, max_aniso=aniso)
+    bad = np.nonzero(got != want)[0]
+    assert bad.size == 0, (bad.size, q[bad[:3]], got[bad[:3]], want[bad[:3]])
