@@ -14,8 +14,10 @@ events around each frame, L2 flushed with a 256 MiB write before every frame); M
 reported beside it.  `e2e` repeats the measurement through the public API with the
 step's vertex/index buffers copied host->device from pinned memory and the colour buffer
 copied back inside the timed region.  `--impl reference` times the reference algorithm on
-the host cores instead (the CPU oracle port; the reference's own sources are not on the
-benchmark machine).  With N > 1 (torchrun) every rank renders the same frames on its own
+the host cores instead: the reference library compiled from its own sources where that
+build exists on the machine (oracle/_ref), else the CPU oracle port (the same OpenMP placement; at one
+thread it skips OpenMP's team fork per triangle and runs as fast as the reference built
+without OpenMP).  With N > 1 (torchrun) every rank renders the same frames on its own
 GPU: replicas, no collective on the data path.
 """
 import argparse
@@ -112,11 +114,24 @@ def frame_bytes(n_idx, vertex_bytes, pixels, frags, passes, texel_bytes=0):
     return 4 * n_idx + vertex_bytes + 8 * pixels + 4 * frags + 8 * passes + texel_bytes * frags
 
 
-def cpu_baseline(min_seconds=10.0, max_frames=32):
-    """The reference algorithm (CPU oracle port) on host cores, best of 1 thread and all."""
+def cpu_engine():
+    """The CPU implementation timed as the reference: the reference library itself
+    (oracle/_ref, compiled from its own sources with OpenMP) where it was built on this
+    machine, else the oracle port (its operation-for-operation restatement, same OpenMP
+    placement).  The reference's sources are not on every benchmark machine."""
     from oracle import oracle
+    if os.path.exists(oracle.PATHS["ref"]):
+        try:
+            return oracle.load("ref"), "reference"
+        except OSError:
+            pass
+    return oracle.load("port"), "port"
+
+
+def cpu_baseline(min_seconds=10.0, max_frames=32):
+    """The reference algorithm on host cores, best of 1 thread and all."""
     from softwarerenderer_gb300 import scenes
-    port = oracle.load("port")
+    port, kind = cpu_engine()
     ncores = os.cpu_count() or 1
     results = {}
     for threads in sorted({1, ncores}):
@@ -132,19 +147,25 @@ def cpu_baseline(min_seconds=10.0, max_frames=32):
         results[threads] = (frags / t_tot / 1e9, n, t_tot, 327680 * n / t_tot / 1e6)
     best = max(results, key=lambda k: results[k][0])
     v, n, t, mtris = results[best]
-    # the reference's Benchmark.cpp program: one drawElements of its scene, wall time
+    # the reference's Benchmark.cpp program: one drawElements of its scene, wall time, the
+    # better of 1 thread and every thread (Span mode gains nothing from OpenMP)
     bsc = scenes.benchmark_scene()
-    btg = scenes.Target(bsc, aux=False)
-    t0 = time.perf_counter()
-    bst = port.draw(bsc, btg, threads=ncores)
-    bms = (time.perf_counter() - t0) * 1e3
-    return {"value": v, "unit": "Gfrags/s", "cores": best, "kind": "port",
+    bres = {}
+    for threads in sorted({1, ncores}):
+        btg = scenes.Target(bsc, aux=False)
+        t0 = time.perf_counter()
+        bst = port.draw(bsc, btg, threads=threads)
+        bres[threads] = ((time.perf_counter() - t0) * 1e3, int(bst["fragments"]))
+    bth = min(bres, key=lambda k: bres[k][0])
+    bms, bfr = bres[bth]
+    return {"value": v, "unit": "Gfrags/s", "cores": best, "kind": kind,
             "sample": f"{n} of the 32 poses, {t:.1f} s of CPU time at {best} thread(s) "
                       f"(best of 1 and {ncores} threads; OpenMP as in the reference)",
             "mtris_per_s": mtris,
             "by_threads": {str(k): round(r[0], 4) for k, r in results.items()},
-            "benchmark_program": {"ms": round(bms, 1), "threads": ncores, "fragments": int(bst["fragments"]),
-                                  "gfrags_per_s": round(bst["fragments"] / (bms / 1e3) / 1e9, 4)}}
+            "benchmark_program": {"ms": round(bms, 1), "threads": bth, "fragments": bfr,
+                                  "gfrags_per_s": round(bfr / (bms / 1e3) / 1e9, 4),
+                                  "ms_by_threads": {str(k): round(r[0], 1) for k, r in bres.items()}}}
 
 
 def run_reference(args, rank):
@@ -155,9 +176,8 @@ def run_reference(args, rank):
     triangles makes every-thread runs slower than one thread)."""
     if rank != 0:
         return
-    from oracle import oracle
     from softwarerenderer_gb300 import scenes
-    port = oracle.load("port")
+    port, kind = cpu_engine()
     allc = os.cpu_count() or 1
     # the first warm-up frame (cold caches, thread-pool start) is not compared; the order of
     # the thread counts alternates so neither always follows the other's idle spin-wait
@@ -180,13 +200,15 @@ def run_reference(args, rank):
         t_tot += time.perf_counter() - t0
         frags += st["fragments"]
     value = frags / t_tot / 1e9
-    cb = {"value": value, "unit": "Gfrags/s", "cores": ncores, "kind": "port",
+    cb = {"value": value, "unit": "Gfrags/s", "cores": ncores, "kind": kind,
           "sample": f"{args.steps} frames (poses 0..{min(args.steps, 32) - 1}), {t_tot:.1f} s"}
     line = {"metric": METRIC, "value": value, "unit": "Gfrags/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_tot / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded icosphere and poses)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "engine": "CPU oracle port of VertexProcessor+Rasterizer",
+            "config": {"workload": WORKLOAD,
+                       "engine": ("the reference library (VertexProcessor+Rasterizer) compiled with OpenMP"
+                                  if kind == "reference" else "CPU oracle port of VertexProcessor+Rasterizer"),
                        "threads": ncores, "threads_tried": counts},
             "mtris_per_s": 327680 * args.steps / t_tot / 1e6,
             "cpu_baseline": cb,
@@ -397,6 +419,7 @@ def run_batched(torch, n=256, steps=10):
     scs = scenes.batch_scenes(n)
     best = autotune.tune(scs)
     br = BatchRenderer(scs, tile=best["tile"], graph=best["graph"], pooled=True)
+    autotune.apply_capacity(br, best["capacity"], (best["need"]["primitives"], best["need"]["bin_entries"]))
     res = {"n_views": n, "triangles_per_step": int(sum(len(x.indices) // 3 for x in scs)),
            "pixels_per_step": int(sum(x.width * x.height for x in scs)), "autotune": best}
     for mode in ("batch", "loop"):

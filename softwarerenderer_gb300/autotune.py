@@ -1,8 +1,18 @@
-"""Autotuner for batched rendering: times the candidate configurations of a batch layout
-(screen tile edge 16 / 32 px, CUDA-graph replay on / off) on the current GPU and caches
-the fastest in softwarerenderer_gb300/_build/autotune.json, keyed by the layout signature
-and the GPU name.  Scratch-queue capacities are sized by the first (warm-up) draw of each
-candidate, which grows the context's queues to exactly what the batch needs."""
+"""Autotuner for batched rendering: times every configuration of a batch layout on the
+current GPU and caches the fastest in softwarerenderer_gb300/_build/autotune.json, keyed by
+the layout signature and the GPU name.
+
+Axes (the full product is timed and reported in `tried`):
+  tile      screen tile edge of the bin/tile rasterizer: 16 or 32 px (a tile is one CTA)
+  graph     CUDA-graph capture and replay of the batch's kernel sequence, or plain launches
+  capacity  how the primitive and bin-entry queues are sized:
+              "grown"  automatically: sized from the submitted triangle count and grown
+                       after a draw overflows them (one retried draw)
+              "exact"  pre-sized once to what this batch needs (swr_set_queue_capacity)
+              "2x"     pre-sized to twice that
+            The bin-entry queue's size also sets the primitive segments of the binning
+            (a segment spans capacity / 32 primitive ids), so it changes the sort work.
+"""
 import hashlib
 import json
 import os
@@ -11,7 +21,9 @@ import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "_build", "autotune.json")
-CANDIDATES = [{"tile": 16, "graph": True}, {"tile": 32, "graph": True}, {"tile": 16, "graph": False}]
+TILES = (16, 32)
+GRAPHS = (True, False)
+CAPACITIES = ("grown", "exact", "2x")
 
 
 def signature(scenes):
@@ -41,8 +53,26 @@ def _time(br, reps):
         br.draw(sync=False)
     e.record()
     torch.cuda.synchronize()
-    br.ctx.finish()
+    rc, _ = br.ctx.finish()
+    assert rc == 0, rc
     return s.elapsed_time(e) / reps
+
+
+def needed_capacity(br):
+    """Primitive and bin-entry counts of one draw of the batch (after any retry)."""
+    br.clear()
+    st = br.draw()
+    return int(st["primitives"]), int(st["bin_pairs"])
+
+
+def apply_capacity(br, capacity, need):
+    """Configure a renderer's queues for one `capacity` setting (see the module doc)."""
+    prims, pairs = need
+    if capacity == "grown":
+        br.ctx.set_queue_capacity(0, 0)
+    else:
+        k = 1 if capacity == "exact" else 2
+        br.ctx.set_queue_capacity(max(1, k * prims), max(1, k * pairs))
 
 
 def tune(scenes, reps=3, force=False):
@@ -53,13 +83,21 @@ def tune(scenes, reps=3, force=False):
     if key in cache and not force:
         return cache[key]
     results = []
-    for cand in CANDIDATES:
-        br = BatchRenderer(scenes, tile=cand["tile"], graph=cand["graph"], pooled=True)
-        ms = _time(br, reps)
-        results.append((ms, cand))
+    need = None
+    for tile in TILES:
+        br = BatchRenderer(scenes, tile=tile, graph=True, pooled=True)
+        if need is None:
+            need = needed_capacity(br)
+        for capacity in CAPACITIES:
+            for graph in GRAPHS:
+                br.ctx.set_graph_mode(graph)
+                apply_capacity(br, capacity, need)
+                ms = _time(br, reps)
+                results.append((ms, {"tile": tile, "graph": graph, "capacity": capacity}))
         del br
     ms, best = min(results, key=lambda r: r[0])
-    entry = dict(best, ms=round(ms, 4), tried=[dict(c, ms=round(t, 4)) for t, c in results])
+    entry = dict(best, ms=round(ms, 4), need={"primitives": need[0], "bin_entries": need[1]},
+                 tried=[dict(c, ms=round(t, 4)) for t, c in results])
     cache[key] = entry
     os.makedirs(os.path.dirname(CACHE), exist_ok=True)
     with open(CACHE, "w") as f:

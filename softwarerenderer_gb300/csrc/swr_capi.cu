@@ -43,6 +43,7 @@ constexpr int kStageCopyBlocks = 8;
 static_assert(sizeof(SwrDrawDesc) % 4 == 0 && sizeof(SwrTargetDesc) % 4 == 0, "descriptors copy as words");
 
 __global__ void k_stage_copy(const StageCopy sc) {
+  swr_pdl_entry();
   for (int k = 0; k < sc.n; ++k) {
     const uint32_t* s = (const uint32_t*)sc.src[k];
     uint32_t* d = (uint32_t*)sc.dst[k];
@@ -50,7 +51,10 @@ __global__ void k_stage_copy(const StageCopy sc) {
   }
 }
 
-__global__ void k_close_draw(uint32_t* st) { swr_close_status(st); }
+__global__ void k_close_draw(uint32_t* st) {
+  swr_pdl_entry();
+  swr_close_status(st);
+}
 
 // Device bytes a context holds, and the cap swr_set_memory_limit puts on them (0: none).
 struct MemBudget {
@@ -329,12 +333,10 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // is allocated and reset by k_sort_big's last block, which also closes the draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
-  k_sort_cells<<<(ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s>>>(
-      st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
+  swr::launch(k_sort_cells, (ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s, st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
       big, (uint32_t)SWR_RASTER_SORT);
   if (use_big) {
-    k_sort_big<<<kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s>>>(
-        st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
+    swr::launch(k_sort_big, kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s, st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
     c->launches += 1;
   }
   mark(c, 4, s);
@@ -359,7 +361,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   if (ra.slices > 1) c->launches += 1;  // k_merge_slices
   mark(c, 5, s);
   if (!use_big) {
-    k_close_draw<<<1, 1, 0, s>>>(st);
+    swr::launch(k_close_draw, 1, 1, 0, s, st);
     c->launches += 1;
   }
   c->launches += 1 + 2 + 1 + 1 + (ntiles ? 1 : 0);
@@ -430,7 +432,7 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
   sh.status_w = st;
   ps->lp_shade(sh, s);
   mark(c, 5, s);
-  k_close_draw<<<1, 1, 0, s>>>(st);
+  swr::launch(k_close_draw, 1, 1, 0, s, st);
   c->launches += 1 + 2 + 1 + 3 * ((bits + 7) / 8) + 1 + 1;
   return cuda_err(cudaGetLastError());
 }
@@ -457,7 +459,7 @@ int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, 
   sc.n = 0;
   sc.add(c->draws.p, h, sizeof(D));
   sc.add(c->targets.p, h + sizeof(D), sizeof(T));
-  k_stage_copy<<<1, 256, 0, s>>>(sc);
+  swr::launch(k_stage_copy, 1, 256, 0, s, sc);
   c->launches += 1;
   cudaEventRecord(c->single_ev[slot], s);
   c->single_pending[slot] = true;
@@ -736,7 +738,7 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
     vs->assemble_emit(aa, nbatches, s);  // derives batch bases and the primitive count itself
   } else {
     vs->assemble_lp_count(aa, nbatches, s);
-    k_batch_scan<<<1, 1024, 0, s>>>(c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
+    swr::launch(k_batch_scan, 1, 1024, 0, s, c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
                                     c->cap_prims);
     vs->assemble_lp_emit(aa, nbatches, s);
   }
@@ -777,10 +779,10 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   c->launches += (nverts ? 1 : 0) + (nsub ? 4 : 0);
   if (nsub) {
     const int grid = (int)((nsub + 255) / 256 < 1216 ? (nsub + 255) / 256 : 1216);
-    k_direct_flags<<<grid, 256, 0, s>>>(indices, nsub, per, c->direct_keep.as<uint32_t>());
+    swr::launch(k_direct_flags, grid, 256, 0, s, indices, nsub, per, c->direct_keep.as<uint32_t>());
     scan_exclusive(c->direct_keep.as<uint32_t>(), c->direct_pos.as<uint32_t>(), nullptr, nsub,
                    st + SWR_ST_PRIMS, c->scratch.as<uint32_t>(), s);
-    k_direct_emit<<<grid, 256, 0, s>>>(indices, nsub, per, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
+    swr::launch(k_direct_emit, grid, 256, 0, s, indices, nsub, per, (uint32_t)nverts, c->direct_keep.as<uint32_t>(),
                                        c->direct_pos.as<uint32_t>(), c->tris.as<uint4>(), st);
   }
   mark(c, 2, s);
@@ -957,7 +959,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
     sc.add(c->draw_vbase.p, h + o_vb, 4 * n);
     sc.add(c->draw_bbase.p, h + o_bb, 4 * n);
     sc.add(c->target_tile_base.p, h + o_tb, 4 * ntg);
-    k_stage_copy<<<kStageCopyBlocks, 256, 0, s>>>(sc);
+    swr::launch(k_stage_copy, kStageCopyBlocks, 256, 0, s, sc);
     c->launches += 1;
     q = cuda_err(cudaGetLastError());
   }

@@ -29,6 +29,7 @@ __device__ __forceinline__ void chunk_range(uint32_t n, uint32_t chunk, uint32_t
 __global__ void __launch_bounds__(kThreads) k_scan_reduce(const uint32_t* in, const uint32_t* n_dev,
                                                           uint32_t n_max, uint32_t chunk,
                                                           uint32_t* partials) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[32];
   const uint32_t n = load_n(n_dev, n_max);
   uint32_t b, e;
@@ -44,6 +45,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* in, uint
                                                         const uint32_t* n_dev, uint32_t n_max,
                                                         uint32_t chunk, const uint32_t* partials,
                                                         uint32_t* total) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[32];
   const uint32_t n = load_n(n_dev, n_max);
   uint32_t b, e;
@@ -98,6 +100,7 @@ constexpr int kWarps = kThreads / 32;
 __global__ void __launch_bounds__(kThreads) k_radix_hist(const uint32_t* keys, const uint32_t* n_dev,
                                                          uint32_t n_max, uint32_t chunk, int shift,
                                                          uint32_t* hist, int nblocks) {
+  swr_pdl_entry();
   __shared__ uint32_t cnt[256];
   cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -113,6 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(const uint32_t* keys, c
 // off[b][d] = digit-d keys in blocks before b; tot[d] = all digit-d keys.
 __global__ void __launch_bounds__(256) k_radix_offsets(const uint32_t* hist, uint32_t* off, uint32_t* tot,
                                                        int nblocks) {
+  swr_pdl_entry();
   const int d = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   uint32_t run = 0;
   for (int b0 = 0; b0 < nblocks; b0 += 32) {
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* kin,
                                                             const uint32_t* n_dev, uint32_t n_max,
                                                             uint32_t chunk, int shift,
                                                             const uint32_t* off, const uint32_t* tot) {
+  swr_pdl_entry();
   __shared__ uint32_t wcnt[kWarps][256];
   __shared__ uint32_t base[256];
   __shared__ uint32_t tile_tot[256];
@@ -200,6 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* kin,
 
 __global__ void k_segment_starts(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max,
                                  uint32_t ntiles, uint32_t* start) {
+  swr_pdl_entry();
   const uint32_t n = load_n(n_dev, n_max);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
     const uint32_t kc = i < n ? keys[i] : ntiles;
@@ -215,8 +221,8 @@ size_t scan_scratch_words(uint32_t) { return kScanBlocks; }
 void scan_exclusive(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_max,
                     uint32_t* total, uint32_t* scratch, cudaStream_t s) {
   const uint32_t chunk = chunk_for(n_max, kScanBlocks);
-  k_scan_reduce<<<kScanBlocks, kThreads, 0, s>>>(in, n_dev, n_max, chunk, scratch);
-  k_scan_down<<<kScanBlocks, kThreads, 0, s>>>(in, out, n_dev, n_max, chunk, scratch, total);
+  swr::launch(k_scan_reduce, kScanBlocks, kThreads, 0, s, in, n_dev, n_max, chunk, scratch);
+  swr::launch(k_scan_down, kScanBlocks, kThreads, 0, s, in, out, n_dev, n_max, chunk, scratch, total);
 }
 
 size_t sort_scratch_words(uint32_t) { return 2 * 256 * kSortBlocks + 256; }
@@ -233,9 +239,9 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, con
     uint32_t* vi = cur ? v1 : v0;
     uint32_t* ko = cur ? k0 : k1;
     uint32_t* vo = cur ? v0 : v1;
-    k_radix_hist<<<kSortBlocks, kThreads, 0, s>>>(ki, n_dev, n_max, chunk, shift, hist, kSortBlocks);
-    k_radix_offsets<<<32, 256, 0, s>>>(hist, off, tot, kSortBlocks);
-    k_radix_scatter<<<kSortBlocks, kThreads, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, chunk, shift, off, tot);
+    swr::launch(k_radix_hist, kSortBlocks, kThreads, 0, s, ki, n_dev, n_max, chunk, shift, hist, kSortBlocks);
+    swr::launch(k_radix_offsets, 32, 256, 0, s, hist, off, tot, kSortBlocks);
+    swr::launch(k_radix_scatter, kSortBlocks, kThreads, 0, s, ki, vi, ko, vo, n_dev, n_max, chunk, shift, off, tot);
     cur ^= 1;
   }
   return cur;
@@ -245,7 +251,7 @@ void segment_starts(const uint32_t* keys, const uint32_t* n_dev, uint32_t n_max,
                     uint32_t* start, cudaStream_t s) {
   const uint32_t want = (n_max + 1 + 255) / 256;
   const int grid = (int)(want < 8192u ? want : 8192u);
-  k_segment_starts<<<grid, 256, 0, s>>>(keys, n_dev, n_max, ntiles, start);
+  swr::launch(k_segment_starts, grid, 256, 0, s, keys, n_dev, n_max, ntiles, start);
 }
 
 }  // namespace swr

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 #include "swr_programs.h"
 
 #define SWR_BATCH_PRIMS 1024  // VertexProcessor flushes every 1024 primitives (VertexProcessor.cpp:110-116)
@@ -48,6 +50,47 @@ enum SwrStatusFlags {
 };
 #define SWR_F_ANY_OVERFLOW (SWR_F_CLIP_OVERFLOW | SWR_F_PRIM_OVERFLOW | SWR_F_PAIR_OVERFLOW | SWR_F_FRAG_OVERFLOW)
 #define SWR_ST_STICKY 8  // words SWR_ST_STICKY + i keep the largest value word i reached (i = CLIP_SLOTS..FRAGS)
+
+// Programmatic dependent launch.  Kernels of a draw are launched so that the next one may
+// become resident while the one before it drains (swr::launch); each such kernel begins
+// with swr_pdl_entry(): it waits until every kernel before it on the stream has completed
+// and its writes are visible (griddepcontrol.wait, a no-op for a kernel launched without
+// the attribute), then lets its own dependents launch.  Nothing of a draw's memory is
+// touched before the wait, so the order of all reads and writes is unchanged.
+__device__ __forceinline__ void swr_pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+namespace swr {
+
+// Launch with the programmatic-stream-serialization attribute (unless SWR_PDL=0 is set in
+// the environment, which launches every kernel fully serialised, as <<<...>>> does).
+inline bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("SWR_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <typename... P, typename... A>
+inline void launch(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, ((P)args)...);
+}
+
+}  // namespace swr
 
 // End of a draw: the sticky maxima of the queue sizes it requested (the host grows its
 // queues from them after an overflow).  One thread, after every stage that counts.

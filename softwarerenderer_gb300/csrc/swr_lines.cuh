@@ -104,6 +104,7 @@ __device__ uint32_t assemble_lp_one(const AssembleArgs& g, const SwrDrawDesc& D,
 
 template <int A, int P>
 __global__ void __launch_bounds__(256) k_assemble_lp_count(AssembleArgs g) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[32];
   const uint32_t b = blockIdx.x;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(256) k_assemble_lp_count(AssembleArgs g) {
 }
 
 static __global__ void __launch_bounds__(256) k_assemble_lp_emit(AssembleArgs g) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[32];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t b = blockIdx.x;
@@ -146,6 +148,7 @@ static __global__ void __launch_bounds__(256) k_assemble_lp_emit(AssembleArgs g)
 // Per primitive: start vertex and per-step increment (computeVertexStep, Rasterizer.h:210-222).
 template <class PS>
 __global__ void __launch_bounds__(256) k_lp_setup(SetupArgs g) {
+  swr_pdl_entry();
   typedef LpRec<PS> RL;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   uint32_t np = g.status[SWR_ST_PRIMS];
@@ -212,6 +215,7 @@ struct LpFragArgs {
 
 template <class PS>
 __global__ void __launch_bounds__(256) k_lp_frags(LpFragArgs g) {
+  swr_pdl_entry();
   typedef LpRec<PS> RL;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t nf = *g.nfrags;
@@ -269,6 +273,7 @@ struct LpShadeArgs {
 
 template <class PS>
 __global__ void __launch_bounds__(256) k_lp_shade(LpShadeArgs g) {
+  swr_pdl_entry();
   typedef LpRec<PS> RL;
   __shared__ uint32_t sfr[32];
   uint32_t frags = 0, passes = 0;

@@ -15,12 +15,12 @@ void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {
   if (!n) return;
   const uint32_t want = (n + 255) / 256;
   const int grid = (int)(want < (uint32_t)kGrid ? want : (uint32_t)kGrid);
-  k_direct_vertices<PS::AVarCount, PS::PVarCount><<<grid, 256, 0, s>>>(rv, n, ptv);
+  swr::launch(k_direct_vertices<PS::AVarCount, PS::PVarCount>, grid, 256, 0, s, rv, n, ptv);
 }
 
 template <class PS>
 void run_setup(const SetupArgs& a, cudaStream_t s) {
-  k_setup<PS><<<kGrid, kSetupThreads, 0, s>>>(a);
+  swr::launch(k_setup<PS>, kGrid, kSetupThreads, 0, s, a);
 }
 
 template <class PS>
@@ -28,7 +28,7 @@ void run_pairs(const uint32_t* status, uint32_t cap_prims, const float* recs, co
                const uint32_t* pair_off, const uint32_t* npairs, uint32_t cap_pairs,
                const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* keys,
                uint32_t* vals, uint32_t* status_w, cudaStream_t s) {
-  k_emit_pairs<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, tile_count, pair_off, npairs, cap_pairs,
+  swr::launch(k_emit_pairs<PS>, kGrid, 256, 0, s, status, cap_prims, recs, tile_count, pair_off, npairs, cap_pairs,
                                          draws, targets, tile, keys, vals, status_w);
 }
 
@@ -37,7 +37,7 @@ void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs,
               uint32_t* cell_count, const uint32_t* cell_start, uint32_t ncells, int seg_shift, uint32_t cap_pairs,
               const SwrDrawDesc* draws, const SwrTargetDesc* targets, int tile, uint32_t* bin, uint32_t* status_w,
               cudaStream_t s) {
-  k_fill_bins<PS><<<kGrid, 256, 0, s>>>(status, cap_prims, recs, cell_count, cell_start, ncells,
+  swr::launch(k_fill_bins<PS>, kGrid, 256, 0, s, status, cap_prims, recs, cell_count, cell_start, ncells,
                                         seg_shift, cap_pairs, draws, targets, tile, bin, status_w);
 }
 
@@ -49,31 +49,31 @@ void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) 
   const bool sliced = SwrOverwrite<PS>::value && a.slices > 1;
   const uint32_t grid = sliced ? ntiles * (uint32_t)a.slices : ntiles;
   if (tile == 32) {
-    if (a.has_span) k_raster<PS, 32, kChunk, true><<<grid, 256, 0, s>>>(a);
-    else k_raster<PS, 32, kChunk, false><<<grid, 256, 0, s>>>(a);
+    if (a.has_span) swr::launch(k_raster<PS, 32, kChunk, true>, grid, 256, 0, s, a);
+    else swr::launch(k_raster<PS, 32, kChunk, false>, grid, 256, 0, s, a);
     if constexpr (SwrOverwrite<PS>::value)
-      if (sliced) k_merge_slices<PS, 32><<<ntiles, 256, 0, s>>>(a);
+      if (sliced) swr::launch(k_merge_slices<PS, 32>, ntiles, 256, 0, s, a);
   } else {
-    if (a.has_span) k_raster<PS, 16, kChunk, true><<<grid, 256, 0, s>>>(a);
-    else k_raster<PS, 16, kChunk, false><<<grid, 256, 0, s>>>(a);
+    if (a.has_span) swr::launch(k_raster<PS, 16, kChunk, true>, grid, 256, 0, s, a);
+    else swr::launch(k_raster<PS, 16, kChunk, false>, grid, 256, 0, s, a);
     if constexpr (SwrOverwrite<PS>::value)
-      if (sliced) k_merge_slices<PS, 16><<<ntiles, 256, 0, s>>>(a);
+      if (sliced) swr::launch(k_merge_slices<PS, 16>, ntiles, 256, 0, s, a);
   }
 }
 
 template <class PS>
 void run_lp_setup(const SetupArgs& a, cudaStream_t s) {
-  k_lp_setup<PS><<<kGrid, 256, 0, s>>>(a);
+  swr::launch(k_lp_setup<PS>, kGrid, 256, 0, s, a);
 }
 
 template <class PS>
 void run_lp_frags(const LpFragArgs& a, cudaStream_t s) {
-  k_lp_frags<PS><<<kGrid, 256, 0, s>>>(a);
+  swr::launch(k_lp_frags<PS>, kGrid, 256, 0, s, a);
 }
 
 template <class PS>
 void run_lp_shade(const LpShadeArgs& a, cudaStream_t s) {
-  k_lp_shade<PS><<<kGrid, 256, 0, s>>>(a);
+  swr::launch(k_lp_shade<PS>, kGrid, 256, 0, s, a);
 }
 
 template <class PS>

@@ -65,6 +65,7 @@ template <class VS>
 __global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ draws, int ndraws,
                                                 const uint32_t* __restrict__ draw_vbase,
                                                 uint32_t nverts, float* __restrict__ ptv) {
+  swr_pdl_entry();
   typedef VLayout<VS::AVarCount, VS::PVarCount> L;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nverts; v += gridDim.x * blockDim.x) {
     const int d = ndraws > 1 ? swr_find_le(draw_vbase, ndraws, v) : 0;
@@ -96,6 +97,7 @@ __global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ 
 // already in screen space; convert them to the post-transform layout of the pixel shader.
 template <int A, int P>
 __global__ void k_direct_vertices(const float* __restrict__ rv, uint32_t nverts, float* __restrict__ ptv) {
+  swr_pdl_entry();
   typedef VLayout<A, P> L;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nverts; v += gridDim.x * blockDim.x) {
     const float* s = rv + (size_t)v * 36;
@@ -305,6 +307,7 @@ __device__ __forceinline__ uint32_t batch_count(const SwrDrawDesc& D, uint32_t p
 // survivors: batch_counts[h] = (kept input slots, kept extra fan triangles).
 template <int A, int P>
 __global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[64];
   const uint32_t hb = blockIdx.x, b = hb >> 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
@@ -325,6 +328,7 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
 // Exclusive scan of per-batch totals -> batch bases; primitive total into the status word.
 static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts, uint32_t nbatches, uint32_t* base,
                                                      uint32_t* status, uint32_t cap_prims) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[32];
   uint32_t run = 0;
   for (uint32_t b0 = 0; b0 < nbatches; b0 += 1024) {
@@ -346,6 +350,7 @@ static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts,
 // the primitive count (and flags an undersized primitive queue).
 template <int A, int P>
 __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
+  swr_pdl_entry();
   __shared__ uint32_t tmp[64];
   __shared__ uint32_t tmps[32];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
@@ -436,6 +441,7 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
 // (Rasterizer::drawTriangleList, Rasterizer.h:134-141); others keep their order.
 static __global__ void k_direct_flags(const int32_t* __restrict__ idx, uint32_t nprims, int per,
                                uint32_t* __restrict__ keep) {
+  swr_pdl_entry();
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < nprims; p += gridDim.x * blockDim.x)
     keep[p] = idx[(size_t)per * p] != -1 ? 1u : 0u;
 }
@@ -443,6 +449,7 @@ static __global__ void k_direct_flags(const int32_t* __restrict__ idx, uint32_t 
 static __global__ void k_direct_emit(const int32_t* __restrict__ idx, uint32_t nprims, int per, uint32_t nverts,
                               const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos,
                               uint4* __restrict__ tris, uint32_t* status) {
+  swr_pdl_entry();
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < nprims; p += gridDim.x * blockDim.x) {
     if (!keep[p]) continue;
     uint32_t r[3] = {0, 0, 0};
@@ -547,6 +554,7 @@ constexpr int kSetupThreads = 128;
 
 template <class PS>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
+  swr_pdl_entry();
   typedef Rec<PS> RL;
   __shared__ float4 stage4[kSetupThreads * RL::R / 4];
   float* stage = (float*)stage4;
@@ -758,6 +766,7 @@ __global__ void __launch_bounds__(256) k_emit_pairs(const uint32_t* status, uint
                                                     const SwrDrawDesc* draws, const SwrTargetDesc* targets,
                                                     int tile, uint32_t* keys, uint32_t* vals,
                                                     uint32_t* status_w) {
+  swr_pdl_entry();
   typedef Rec<PS> RL;
   if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   if (*npairs > cap_pairs) {
@@ -797,6 +806,7 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
                                                    uint32_t cap_pairs, const SwrDrawDesc* draws,
                                                    const SwrTargetDesc* targets, int tile, uint32_t* bin,
                                                    uint32_t* status_w) {
+  swr_pdl_entry();
   typedef Rec<PS> RL;
   // cell_count is all zero between draws: every entry counted by k_setup is taken back
   // here, and a draw that stops early zeroes the counts instead
@@ -853,6 +863,7 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
                                                           uint32_t ntiles, uint32_t cap_pairs, const uint32_t* in,
                                                           uint32_t* out, uint32_t* big_list, uint32_t* big_count,
                                                           uint32_t self_sorted) {
+  swr_pdl_entry();
   if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   if (cell_start[(size_t)ntiles * SWR_SEGS] > cap_pairs) return;
   const int lane = threadIdx.x & 31;
@@ -914,6 +925,7 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
 static __global__ void k_sort_big(uint32_t* status, const uint32_t* cell_start, uint32_t ncells,
                                   uint32_t cap_pairs, int seg_shift, const uint32_t* in, uint32_t* out,
                                   const uint32_t* big_list, uint32_t* big_count) {
+  swr_pdl_entry();
   extern __shared__ uint32_t smem_bm[];
   const bool skip = (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) || cell_start[ncells] > cap_pairs;
   const uint32_t nbig = skip ? 0u : min(*(volatile uint32_t*)big_count, ncells);
@@ -1183,6 +1195,7 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 template <class PS, int TILE, int CH, bool SPAN>
 __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRasterOccupancy<PS>::value)
     k_raster(RasterArgs g) {
+  swr_pdl_entry();
   typedef Rec<PS> RL;
   typedef typename PS::Color Color;
   constexpr int PPT = TILE * TILE / 256;  // pixels per thread
@@ -1741,6 +1754,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 // per pixel the slices' States in bin order (swr_overwrite_merge), then the shader's store.
 template <class PS, int TILE>
 __global__ void __launch_bounds__(256) k_merge_slices(RasterArgs g) {
+  swr_pdl_entry();
   constexpr int PPT = TILE * TILE / 256;
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const uint32_t tile = blockIdx.x;

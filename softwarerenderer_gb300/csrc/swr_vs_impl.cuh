@@ -15,26 +15,26 @@ void run_vertex(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase
   if (!nverts) return;
   const uint32_t want = (nverts + 255) / 256;
   const int grid = (int)(want < (uint32_t)kVsGrid ? want : (uint32_t)kVsGrid);
-  k_vertex<VS><<<grid, 256, 0, s>>>(draws, ndraws, draw_vbase, nverts, ptv);
+  swr::launch(k_vertex<VS>, grid, 256, 0, s, draws, ndraws, draw_vbase, nverts, ptv);
 }
 
 template <class VS>
 void run_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_count<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
+  if (nbatches) swr::launch(k_assemble_count<VS::AVarCount, VS::PVarCount>, 2 * nbatches, SWR_HALF, 0, s, a);
 }
 
 template <class VS>
 void run_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_emit<VS::AVarCount, VS::PVarCount><<<2 * nbatches, SWR_HALF, 0, s>>>(a);
+  if (nbatches) swr::launch(k_assemble_emit<VS::AVarCount, VS::PVarCount>, 2 * nbatches, SWR_HALF, 0, s, a);
 }
 
 template <class VS>
 void run_lp_count(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_lp_count<VS::AVarCount, VS::PVarCount><<<nbatches, 256, 0, s>>>(a);
+  if (nbatches) swr::launch(k_assemble_lp_count<VS::AVarCount, VS::PVarCount>, nbatches, 256, 0, s, a);
 }
 
 inline void run_lp_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s) {
-  if (nbatches) k_assemble_lp_emit<<<nbatches, 256, 0, s>>>(a);
+  if (nbatches) swr::launch(k_assemble_lp_emit, nbatches, 256, 0, s, a);
 }
 
 template <class VS>

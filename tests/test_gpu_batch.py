@@ -96,3 +96,20 @@ def test_full_batched_config_matches_oracle(gpu_lib, port):
         assert int(st["fragments"]) == total, (rep, st["fragments"], total)
         for sc, tg, (ref, _) in zip(scs, br.targets, refs):
             assert not diff(ref, tg.to_host()), (rep, sc.name, diff(ref, tg.to_host()))
+
+
+def test_autotuner_covers_tile_capacity_graph(gpu_lib, port):
+    """The autotuner times tile x queue capacity x graph and its choice renders exactly."""
+    from softwarerenderer_gb300 import autotune
+    from softwarerenderer_gb300.batch import BatchRenderer
+    scs = _small_batch(6, seed=45)
+    best = autotune.tune(scs, reps=1, force=True)
+    combos = {(t["tile"], t["capacity"], t["graph"]) for t in best["tried"]}
+    assert combos == {(t, c, g) for t in autotune.TILES for c in autotune.CAPACITIES for g in autotune.GRAPHS}
+    br = BatchRenderer(scs, aux=True, tile=best["tile"], graph=best["graph"])
+    autotune.apply_capacity(br, best["capacity"], (best["need"]["primitives"], best["need"]["bin_entries"]))
+    br.clear()
+    br.draw()
+    for sc, tg in zip(scs, br.targets):
+        ref, _ = oracle_render(port, sc)
+        assert not diff(ref, tg.to_host()), sc.name
