@@ -1229,6 +1229,12 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   static_assert(CH % 32 == 0 && CH <= 128, "chunks of 32, 64, 96 or 128 primitives");
   __shared__ uint32_t sculr[kCull ? NREG * NW : 1];  // per region: primitives only counted there
   __shared__ int sminx[kCull && SPAN ? CH : 1];  // Span mode: leftmost start of a span reaching the tile
+  // Per-pixel walk (shaders without the depth cull or overwrite shortcut): each pixel keeps
+  // the set of compacted primitives covering it (set in C1), so in C2 every lane visits only
+  // its own pixel's primitives instead of all primitives touching its warp's half block.
+  constexpr int HW = (CH + 63) / 64;  // 64-primitive words of a chunk
+  constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !kCull && !SwrOverwrite<PS>::value;
+  __shared__ uint64_t spm[kPixWalk ? TILE * TILE * HW : 1];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
@@ -1309,6 +1315,12 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     __syncthreads();  // the previous chunk's shared state is no longer read; ssorted is complete
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snpart = 0;
+    if constexpr (kPixWalk) {
+#pragma unroll
+      for (int q = 0; q < PPT; ++q)
+#pragma unroll
+        for (int w = 0; w < HW; ++w) spm[((py[q] - oy) * TILE + (px[q] - ox)) * HW + w] = 0ull;
+    }
     if (kCull && SPAN && threadIdx.x < CH) sminx[threadIdx.x] = 0x7fffffff;
     // Region depth bounds at the chunk's start (depth-tested shaders, tiles of more than one
     // chunk): per region an order-preserving key of the largest depth its pixels hold (NaN
@@ -1612,6 +1624,8 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
       sfz[f] = pd.z;
       sfc[f] = PS::shade(pd, g.draws[__float_as_int(r[1])].u);
+      if constexpr (kPixWalk)
+        atomicOr((unsigned long long*)&spm[((y - oy) * TILE + (x - ox)) * HW + (k >> 6)], 1ull << (k & 63));
     }
     __syncthreads();
     // C2: fragments in primitive order.  Each warp owns one 8 x 4 half block per sub-tile
@@ -1620,7 +1634,67 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
       const int half = (py[q] >> 2) & 1;
-      constexpr int HW = (CH + 63) / 64;  // 64-primitive words
+      if constexpr (kPixWalk) {
+        // the warp's primitives that were not compacted and touch its half block (ballot),
+        // plus this pixel's compacted primitives; visited per lane in increasing order
+        uint64_t todo[HW];
+#pragma unroll
+        for (int w = 0; w < HW; ++w) todo[w] = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          const int k = w * 32 + lane;
+          const bool h = k < n && !scomp[k] && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
+          todo[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
+        }
+        if (!in[q]) continue;
+        const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+        const int pix = (py[q] - oy) * TILE + (px[q] - ox);
+#pragma unroll
+        for (int w = 0; w < HW; ++w) {
+          uint64_t t = todo[w] | spm[pix * HW + w];
+          while (t) {
+            const int k = w * 64 + __ffsll((long long)t) - 1;
+            t &= t - 1ull;
+            const uint64_t* mk = smask + k * NB;
+            const uint64_t m = mk[blk[q]];
+            if (!((m >> bit) & 1ull)) continue;
+            const float* r = srec + k * RL::R;
+            frags++;
+            if (scomp[k]) {
+              int rank = __popcll(m & ((1ull << bit) - 1ull));
+              for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
+              const int f = (int)sex[k] + rank;
+              PS::apply(st[q], sfz[f], sfc[f], prim_id(g, r, sids[k]));
+              continue;
+            }
+            const bool blockmode = !SPAN || (__float_as_int(r[0]) & 2);
+            float fx, fy;
+            int ka, kb;
+            if (blockmode) {
+              fx = swr_add((float)(px[q] & ~7), 0.5f);
+              fy = swr_add((float)(py[q] & ~7), 0.5f);
+              ka = px[q] & 7;
+              kb = py[q] & 7;
+            } else {
+              const int2 sp = sspan[k * TILE + (py[q] - oy)];
+              fx = swr_add((float)sp.x, 0.5f);
+              fy = swr_add((float)py[q], 0.5f);
+              ka = px[q] - sp.x;
+              kb = 0;
+            }
+            const float* eq = r + RL::EQ0;
+            GpuPixel<PS> pd;
+            pd.x = px[q];
+            pd.y = py[q];
+            pd.eq = eq;
+            pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
+            if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
+            build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
+            PS::drawPixel(pd, prim_id(g, r, sids[k]), st[q], g.draws[__float_as_int(r[1])].u);
+          }
+        }
+        continue;
+      }
       uint64_t hw[HW];
 #pragma unroll
       for (int w = 0; w < HW; ++w) hw[w] = 0;
