@@ -1233,7 +1233,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   // the set of compacted primitives covering it (set in C1), so in C2 every lane visits only
   // its own pixel's primitives instead of all primitives touching its warp's half block.
   constexpr int HW = (CH + 63) / 64;  // 64-primitive words of a chunk
-  constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !kCull && !SwrOverwrite<PS>::value;
+  constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !SwrOverwrite<PS>::value;
   __shared__ uint64_t spm[kPixWalk ? TILE * TILE * HW : 1];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1646,8 +1646,27 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
           const bool h = k < n && !scomp[k] && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
           todo[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
         }
-        if (!in[q]) continue;
         const int bit = (py[q] & 7) * 8 + (px[q] & 7);
+        if (kCull && scull_on) {
+          // (nothing is compacted in a chunk that culls) primitives culled in this warp's
+          // region fail their depth tests: only counted, in any order (counters commute)
+          const uint32_t* cr = sculr + (q * 8 + warp) * NW;
+#pragma unroll
+          for (int w = 0; w < HW; ++w) {
+            const uint64_t cm = (uint64_t)cr[2 * w] | (2 * w + 1 < NW ? (uint64_t)cr[2 * w + 1] << 32 : 0ull);
+            uint64_t ch = todo[w] & cm;
+            todo[w] &= ~ch;
+            while (ch) {
+              const int k = w * 64 + __ffsll((long long)ch) - 1;
+              ch &= ch - 1ull;
+              if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
+                frags++;
+                PS::earlyReject(__int_as_float(0x7f800000), st[q]);  // counts the rejected fragment
+              }
+            }
+          }
+        }
+        if (!in[q]) continue;
         const int pix = (py[q] - oy) * TILE + (px[q] - ox);
 #pragma unroll
         for (int w = 0; w < HW; ++w) {
