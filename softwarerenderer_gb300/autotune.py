@@ -3,14 +3,15 @@ current GPU and caches the fastest in softwarerenderer_gb300/_build/autotune.jso
 the layout signature and the GPU name.
 
 Axes (the full product is timed and reported in `tried`):
-  tile      screen tile edge of the bin/tile rasterizer: 16 or 32 px (a tile is one CTA)
+  tile      raster tile edge: 32 or 16 px (one CTA per tile; heavy 16-px tiles split into
+            four 8 x 8 CTAs) or 8 px (16-px bins, every tile rasterized as four 8 x 8 CTAs)
   graph     CUDA-graph capture and replay of the batch's kernel sequence, or plain launches
   capacity  how the primitive and bin-entry queues are sized:
               "grown"  automatically: sized from the submitted triangle count and grown
                        after a draw overflows them (one retried draw)
               "exact"  pre-sized once to what this batch needs (swr_set_queue_capacity)
               "2x"     pre-sized to twice that
-            The bin-entry queue's size also sets the primitive segments of the binning
+            The primitive queue's size also sets the primitive segments of the binning
             (a segment spans capacity / 32 primitive ids), so it changes the sort work.
 """
 import hashlib
@@ -21,7 +22,7 @@ import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(HERE, "_build", "autotune.json")
-TILES = (16, 32)
+TILES = (8, 16, 32)
 GRAPHS = (True, False)
 CAPACITIES = ("grown", "exact", "2x")
 

@@ -23,6 +23,15 @@ constexpr size_t kSingleSlotBytes = 1024;  // >= sizeof(SwrDrawDesc) + sizeof(Sw
 constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CTA (bounds one warp's bitmap)
 constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
 constexpr int kStickyBase = SWR_ST_STICKY;
+constexpr uint32_t kQuadMin = 3 * SWR_CHUNK;  // bin entries above which a 16-px tile is split into quadrant CTAs
+
+// Tiles k_sort_cells may list for quadrant CTAs: enough to cover the slow tail of a frame
+// whose heavy tiles are few; every listed tile adds three CTAs.
+uint32_t quad_cap(uint32_t ntiles) {
+  uint32_t cap = ntiles / 8;
+  cap = cap < 152 ? 152 : (cap > 1024 ? 1024 : cap);
+  return cap < ntiles ? cap : ntiles;
+}
 
 // Descriptor upload from pinned host staging (device-accessible under unified addressing)
 // by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
@@ -124,6 +133,8 @@ struct swr_context {
   swr::Buffer tris, recs, tile_count, pair_off, keys0, vals0, keys1, vals1, tile_start;
   swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
   swr::Buffer big_cells;  // k_sort_cells -> k_sort_big: [count, cell ids...]
+  swr::Buffer quad_flag, quad_tiles, quad_count;  // heavy 16-px tiles rasterized as four quadrant CTAs
+  int quad_mode = 1;  // 0: off, 1: heavy tiles (more than kQuadMin entries), 2: every tile (8-px raster tiles)
   swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
   int slices = 1;           // slices the buffer holds for the current tile count
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
@@ -163,7 +174,7 @@ struct swr_context {
                           &clip_table, &clip_slot, &tri_flags, &batch_counts, &batch_base, &tris, &recs,
                           &tile_count, &pair_off, &keys0, &vals0, &keys1, &vals1, &tile_start, &scratch,
                           &status, &direct_keep, &direct_pos, &lp_refs, &cell_count, &cell_start, &draw_pbase,
-                          &big_cells, &slice_state};
+                          &big_cells, &slice_state, &quad_flag, &quad_tiles, &quad_count};
     for (swr::Buffer* b : all) b->budget = &budget;
   }
 };
@@ -237,6 +248,9 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
     ok &= c->cell_count.p && cudaMemset(c->cell_count.p, 0, c->cell_count.bytes) == cudaSuccess;
   }
   ok &= c->cell_start.ensure(((size_t)ntiles * SWR_SEGS + 1) * 4 + 16);
+  ok &= c->quad_flag.ensure((size_t)ntiles + 16);
+  ok &= c->quad_tiles.ensure((size_t)quad_cap(ntiles) * 4 + 16);
+  ok &= c->quad_count.ensure(16);
   if (c->big_cells.bytes < ((size_t)ntiles * SWR_SEGS + 2) * 4) {
     ok &= c->big_cells.ensure(((size_t)ntiles * SWR_SEGS + 2) * 4 + 16);
     // the list length and completion counter start at zero (k_sort_big resets them)
@@ -333,8 +347,15 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // is allocated and reset by k_sort_big's last block, which also closes the draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
+  // heavy-tile quadrant CTAs (16-px tiles, shaders other than the overwrite ones)
+  const bool quads = c->tile == 16 && !ps->overwrite && c->quad_mode != 0;
+  const bool quad_list = quads && c->quad_mode == 1;
+  const uint32_t qcap = quad_cap(ntiles);
+  if (quad_list) cudaMemsetAsync(c->quad_count.p, 0, 4, s);
   swr::launch(k_sort_cells, (ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s, st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
-      big, (uint32_t)SWR_RASTER_SORT);
+      big, (uint32_t)SWR_RASTER_SORT,
+      quad_list ? c->quad_flag.as<uint8_t>() : nullptr, c->quad_tiles.as<uint32_t>(), c->quad_count.as<uint32_t>(), qcap,
+      kQuadMin);
   if (use_big) {
     swr::launch(k_sort_big, kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s, st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
     c->launches += 1;
@@ -357,6 +378,11 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.has_span = has_span ? 1 : 0;
   ra.slices = ps->overwrite ? c->slices : 1;
   ra.slice_state = c->slice_state.p;
+  ra.quad_flag = quad_list ? c->quad_flag.as<uint8_t>() : nullptr;
+  ra.quad_tiles = c->quad_tiles.as<uint32_t>();
+  ra.quad_count = c->quad_count.as<uint32_t>();
+  ra.quad_cap = qcap;
+  ra.quad_all = quads && c->quad_mode == 2;
   ps->raster(ra, ntiles, c->tile, s);
   if (ra.slices > 1) c->launches += 1;  // k_merge_slices
   mark(c, 5, s);
@@ -645,8 +671,15 @@ int swr_memory_used(swr_context* c, uint64_t* bytes) {
 }
 
 int swr_set_tile_size(swr_context* c, int tile) {
-  if (!c || (tile != 16 && tile != 32)) return SWR_EINVAL;
-  c->tile = tile;
+  if (!c || (tile != 8 && tile != 16 && tile != 32)) return SWR_EINVAL;
+  c->tile = tile == 32 ? 32 : 16;  // 8: 16-px bins, every tile rasterized as four 8 x 8 CTAs
+  c->quad_mode = tile == 8 ? 2 : 1;
+  return SWR_OK;
+}
+
+int swr_set_tile_split(swr_context* c, int on) {
+  if (!c) return SWR_EINVAL;
+  if (c->quad_mode != 2) c->quad_mode = on ? 1 : 0;
   return SWR_OK;
 }
 
@@ -925,13 +958,15 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   memcpy(h + o_bb, bbase.data(), 4 * n);
   memcpy(h + o_tb, tbase.data(), 4 * ntg);
   mix((uint64_t)(uintptr_t)vs); mix((uint64_t)(uintptr_t)ps);  // the programs (their kernels)
+  mix((uint64_t)c->quad_mode);
   mix((uint64_t)vs->S); mix((uint64_t)ps->R); mix((uint64_t)c->tile); mix((uint64_t)n);
   mix(c->cap_prims); mix(c->cap_pairs); mix(c->cap_clip_slots); mix(c->cap_clip_verts);
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
                         c->tris.p, c->recs.p, c->tile_count.p, c->keys0.p, c->vals0.p, c->cell_count.p,
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
                         c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage,
-                        c->slice_state.p, (const void*)(uintptr_t)c->slices};
+                        c->slice_state.p, (const void*)(uintptr_t)c->slices, c->quad_flag.p, c->quad_tiles.p,
+                        c->quad_count.p};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
   if (c->graph_mode && c->gexec && sig == c->gsig) {
     if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;

@@ -275,6 +275,11 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.has_span = raster_mode != SWR_RASTER_BLOCK;
   ra.slices = 1;  // no slice buffer without allocation
   ra.slice_state = nullptr;
+  ra.quad_flag = nullptr;  // no heavy-tile quadrant CTAs: every tile is one CTA
+  ra.quad_tiles = nullptr;
+  ra.quad_count = nullptr;
+  ra.quad_cap = 0;
+  ra.quad_all = 0;
   ps->raster(ra, ntiles, kTile, s);
   if (cudaGetLastError() != cudaSuccess) return SWR_ECUDA;  // a launch failed: the status words are stale
   uint32_t h[16];

@@ -47,7 +47,11 @@ void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) 
   // one CTA per tile, or per (tile, slice) for sliced overwrite shaders; Block-only
   // submissions run the instantiation without the Span-mode passes
   const bool sliced = SwrOverwrite<PS>::value && a.slices > 1;
-  const uint32_t grid = sliced ? ntiles * (uint32_t)a.slices : ntiles;
+  uint32_t grid = sliced ? ntiles * (uint32_t)a.slices : ntiles;
+  if (tile == 16 && !SwrOverwrite<PS>::value) {  // quadrant CTAs (RasterArgs)
+    if (a.quad_all) grid = 4 * ntiles;
+    else if (a.quad_flag) grid = 4 * a.quad_cap + ntiles;
+  }
   if (tile == 32) {
     if (a.has_span) swr::launch(k_raster<PS, 32, kChunk, true>, grid, 256, 0, s, a);
     else swr::launch(k_raster<PS, 32, kChunk, false>, grid, 256, 0, s, a);

@@ -862,7 +862,9 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
 static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* status, const uint32_t* cell_start,
                                                           uint32_t ntiles, uint32_t cap_pairs, const uint32_t* in,
                                                           uint32_t* out, uint32_t* big_list, uint32_t* big_count,
-                                                          uint32_t self_sorted) {
+                                                          uint32_t self_sorted, uint8_t* quad_flag,
+                                                          uint32_t* quad_tiles, uint32_t* quad_count,
+                                                          uint32_t quad_cap, uint32_t quad_min) {
   swr_pdl_entry();
   if (status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   if (cell_start[(size_t)ntiles * SWR_SEGS] > cap_pairs) return;
@@ -870,6 +872,18 @@ static __global__ void __launch_bounds__(256) k_sort_cells(const uint32_t* statu
   const uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (t >= ntiles) return;
   const uint32_t last = cell_start[(size_t)t * SWR_SEGS + SWR_SEGS];
+  // heavy tiles: listed for k_raster's quadrant CTAs (quad_count is zeroed before this kernel)
+  if (quad_flag && lane == 0) {
+    uint8_t f = 0;
+    if (last - cell_start[(size_t)t * SWR_SEGS] > quad_min) {
+      const uint32_t slot = atomicAdd(quad_count, 1u);
+      if (slot < quad_cap) {
+        quad_tiles[slot] = t;
+        f = 1;
+      }
+    }
+    quad_flag[t] = f;
+  }
   // tiles of at most `self_sorted` entries are ordered by the raster kernel itself
   if (last - cell_start[(size_t)t * SWR_SEGS] <= self_sorted) return;  // uniform per warp
   const uint32_t s = cell_start[(size_t)t * SWR_SEGS + lane];
@@ -1038,6 +1052,18 @@ struct RasterArgs {
                                      // entries (1: no slicing), each over an ordered slice of its bin
   void* slice_state;                 // their per-pixel PS::State, [tile][slice][TILE * TILE]
   int has_span;                      // some draw rasterizes in Span or Adaptive mode (selects k_raster<..., true>)
+  // Quadrant CTAs (16-px tiles, shaders other than the overwrite ones): a heavy tile -- more
+  // than quad_min bin entries; k_sort_cells lists up to quad_cap of them -- is rasterized by
+  // four CTAs, one per 8 x 8 quadrant, each walking the whole bin for its own pixels, so the
+  // slowest tiles no longer set the kernel's length.  CTAs [0, 4 quad_cap) take the listed
+  // tiles' quadrants first; CTA 4 quad_cap + t takes tile t unless it is listed.  With
+  // quad_all every tile is split (CTA 4 t + q: quadrant q of tile t): an 8-px raster tile
+  // over 16-px bins.
+  const uint8_t* quad_flag;          // per tile: 1 = listed (null: no heavy-tile split)
+  const uint32_t* quad_tiles;        // listed tiles
+  const uint32_t* quad_count;        // tiles k_sort_cells listed (may exceed quad_cap)
+  uint32_t quad_cap;
+  int quad_all;
 };
 
 // v <- fl(v + a) repeated k times for 0 <= k <= 7 (steps inside one 8x8 block), as
@@ -1249,6 +1275,24 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     tile = blockIdx.x / (uint32_t)g.slices;
     slice = blockIdx.x - tile * (uint32_t)g.slices;
   }
+  int quad = -1;  // the 8 x 8 quadrant (block) this CTA rasterizes alone, -1: the whole tile
+  if constexpr (TILE == 16 && !SwrOverwrite<PS>::value) {
+    if (g.quad_all) {
+      tile = blockIdx.x >> 2;
+      quad = (int)(blockIdx.x & 3u);
+    } else if (g.quad_flag) {
+      const uint32_t nq = 4u * g.quad_cap;
+      if (blockIdx.x < nq) {
+        const uint32_t slot = blockIdx.x >> 2;
+        if (slot >= min(*g.quad_count, g.quad_cap)) return;
+        tile = g.quad_tiles[slot];
+        quad = (int)(blockIdx.x & 3u);
+      } else {
+        tile = blockIdx.x - nq;
+        if (tile < g.ntiles && g.quad_flag[tile]) return;  // rasterized by its quadrant CTAs
+      }
+    }
+  }
   if (tile >= g.ntiles) return;
   uint32_t b = g.tile_start[(size_t)tile * g.tile_stride], e = g.tile_start[(size_t)(tile + 1) * g.tile_stride];
   bool sliced = false;
@@ -1285,7 +1329,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     px[q] = ox + lx;
     py[q] = oy + ly;
     blk[q] = (ly >> 3) * NBX + (lx >> 3);
-    in[q] = px[q] < T.width && py[q] < T.height;
+    in[q] = px[q] < T.width && py[q] < T.height && (quad < 0 || blk[q] == quad);
     if (in[q]) PS::load(st[q], px[q], py[q], U);
   }
   // A tile of at most SWR_RASTER_SORT entries orders its own bin: the cells (increasing id
@@ -1368,6 +1412,10 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       const float* r = srec + k * RL::R;
       const int flags = __float_as_int(r[0]);
       if (SPAN && (flags & 3) == 1) continue;  // Span mode: rows below, masks after the barrier
+      if (quad >= 0 && j != quad) {  // another CTA's quadrant
+        smask[i] = 0;
+        continue;
+      }
       const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
       uint64_t m = 0;
       const bool hit = (flags & 1) && bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
@@ -1420,6 +1468,10 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         const float* r = srec + k * RL::R;
         const int flags = __float_as_int(r[0]);
         if ((flags & 3) != 1) continue;
+        if (quad >= 0 && j != quad) {
+          smask[i] = 0;
+          continue;
+        }
         const int bx = ox + (j % NBX) * SWR_BLOCK, by = oy + (j / NBX) * SWR_BLOCK;
         const bool hit = bx <= __float_as_int(r[4]) && bx + SWR_BLOCK - 1 >= __float_as_int(r[2]) &&
                          by <= __float_as_int(r[5]) && by + SWR_BLOCK - 1 >= __float_as_int(r[3]);

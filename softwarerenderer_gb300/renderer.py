@@ -91,6 +91,12 @@ class Context:
         _lib.check(L.swr_memory_used(self.h, ctypes.byref(v)), "memory_used")
         return int(v.value)
 
+    def set_tile_split(self, on=True):
+        """Heavy 16-px tiles rasterized as four 8 x 8 quadrant CTAs (the default) or whole."""
+        self.L.swr_set_tile_split.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.swr_set_tile_split.restype = ctypes.c_int
+        _lib.check(self.L.swr_set_tile_split(self.h, int(bool(on))), "set_tile_split")
+
     def set_profiling(self, on=True):
         _lib.check(self.L.swr_set_profiling(self.h, int(bool(on))), "set_profiling")
 

@@ -19,9 +19,9 @@ pytestmark = pytest.mark.gpu
 TRI_SEEDS = list(range(0, 160))
 
 
-def _check(port, sc, tile=16):
+def _check(port, sc, tile=16, split=True):
     ref, rst = oracle_render(port, sc)
-    got, gst = gpu_render(sc, tile=tile)
+    got, gst = gpu_render(sc, tile=tile, split=split)
     bad = diff(ref, got)
     msgs = [describe(ref, got, k) for k in bad]
     assert not bad, f"{sc.name} {sc.draw_mode.name} {sc.raster.name}: " + "; ".join(msgs)
@@ -39,6 +39,22 @@ def test_random_triangles(gpu_lib, port, seed):
 def test_random_triangles_tile32(gpu_lib, port, seed):
     sc = scenes.random_scene(1000 + seed, draw_mode=DrawMode.Triangle)
     _check(port, sc, tile=32)
+
+
+@pytest.mark.parametrize("seed", range(0, 24))
+def test_random_triangles_tile8(gpu_lib, port, seed):
+    """8-px raster tiles: 16-px bins, every tile rasterized as four 8 x 8 quadrant CTAs."""
+    sc = scenes.random_scene(2000 + seed, draw_mode=DrawMode.Triangle)
+    _check(port, sc, tile=8)
+
+
+@pytest.mark.parametrize("tile,split", [(8, True), (16, False), (32, True)])
+def test_heavy_tiles_split_or_whole(gpu_lib, port, tile, split):
+    """The dense mesh's silhouette tiles (hundreds of bin entries) and the dense soup: by
+    quadrant CTAs (tile 8, and tile 16's default heavy-tile split) and whole."""
+    _check(port, scenes.sphere_scene(8), tile=tile, split=split)
+    sc = scenes.soup_scene(1 << 14, width=320, height=240, seed=12, raster=RasterMode.Adaptive)
+    _check(port, sc, tile=tile, split=split)
 
 
 @pytest.mark.parametrize("frame", [0, 1, 17, 42, 99])
