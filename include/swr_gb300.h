@@ -167,9 +167,10 @@ SWR_API int swr_get_queue_capacity(swr_context* ctx, uint64_t* primitives, uint6
 SWR_API int swr_set_memory_limit(swr_context* ctx, uint64_t bytes);
 SWR_API int swr_memory_used(swr_context* ctx, uint64_t* bytes);
 /* Screen tile edge of the bin/tile rasterizer: 16 or 32 pixels, or 8: 16-px bins with every
- * tile rasterized as four 8 x 8 CTAs.  With 16-px tiles, heavy tiles (more than three
- * raster chunks of bin entries) are rasterized as four 8 x 8 CTAs by default, so a few
- * slow tiles do not set the frame's length; swr_set_tile_split(ctx, 0) turns that off. */
+ * tile rasterized as four 8 x 8 CTAs.  swr_set_tile_split(ctx, 1) rasterizes only the heavy
+ * 16-px tiles (more than three raster chunks of bin entries) as four 8 x 8 CTAs; off by
+ * default (each such CTA still stages the whole bin, which costs more than it saves on the
+ * measured workloads). */
 SWR_API int swr_set_tile_size(swr_context* ctx, int tile);
 SWR_API int swr_set_tile_split(swr_context* ctx, int on);
 SWR_API const char* swr_status_string(int status);

@@ -3,8 +3,8 @@ current GPU and caches the fastest in softwarerenderer_gb300/_build/autotune.jso
 the layout signature and the GPU name.
 
 Axes (the full product is timed and reported in `tried`):
-  tile      raster tile edge: 32 or 16 px (one CTA per tile; heavy 16-px tiles split into
-            four 8 x 8 CTAs) or 8 px (16-px bins, every tile rasterized as four 8 x 8 CTAs)
+  tile      raster tile edge: 32 or 16 px (one CTA per tile) or 8 px (16-px bins, every tile
+            rasterized as four 8 x 8 CTAs)
   graph     CUDA-graph capture and replay of the batch's kernel sequence, or plain launches
   capacity  how the primitive and bin-entry queues are sized:
               "grown"  automatically: sized from the submitted triangle count and grown

@@ -134,7 +134,7 @@ struct swr_context {
   swr::Buffer scratch, status, direct_keep, direct_pos, lp_refs, cell_count, cell_start, draw_pbase;
   swr::Buffer big_cells;  // k_sort_cells -> k_sort_big: [count, cell ids...]
   swr::Buffer quad_flag, quad_tiles, quad_count;  // heavy 16-px tiles rasterized as four quadrant CTAs
-  int quad_mode = 1;  // 0: off, 1: heavy tiles (more than kQuadMin entries), 2: every tile (8-px raster tiles)
+  int quad_mode = 0;  // 0: off, 1: heavy tiles (more than kQuadMin entries), 2: every tile (8-px raster tiles)
   swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
   int slices = 1;           // slices the buffer holds for the current tile count
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
@@ -673,7 +673,7 @@ int swr_memory_used(swr_context* c, uint64_t* bytes) {
 int swr_set_tile_size(swr_context* c, int tile) {
   if (!c || (tile != 8 && tile != 16 && tile != 32)) return SWR_EINVAL;
   c->tile = tile == 32 ? 32 : 16;  // 8: 16-px bins, every tile rasterized as four 8 x 8 CTAs
-  c->quad_mode = tile == 8 ? 2 : 1;
+  c->quad_mode = tile == 8 ? 2 : 0;
   return SWR_OK;
 }
 

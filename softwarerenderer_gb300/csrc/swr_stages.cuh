@@ -1686,7 +1686,9 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
       const int half = (py[q] >> 2) & 1;
-      if constexpr (kPixWalk) {
+      // Chunks whose depth cull is on compact nothing: every primitive then goes through the
+      // warp-uniform walk below, which costs less than per-lane loops over the same list.
+      if (kPixWalk && !(kCull && scull_on)) {
         // the warp's primitives that were not compacted and touch its half block (ballot),
         // plus this pixel's compacted primitives; visited per lane in increasing order
         uint64_t todo[HW];
@@ -1699,25 +1701,6 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
           todo[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
         }
         const int bit = (py[q] & 7) * 8 + (px[q] & 7);
-        if (kCull && scull_on) {
-          // (nothing is compacted in a chunk that culls) primitives culled in this warp's
-          // region fail their depth tests: only counted, in any order (counters commute)
-          const uint32_t* cr = sculr + (q * 8 + warp) * NW;
-#pragma unroll
-          for (int w = 0; w < HW; ++w) {
-            const uint64_t cm = (uint64_t)cr[2 * w] | (2 * w + 1 < NW ? (uint64_t)cr[2 * w + 1] << 32 : 0ull);
-            uint64_t ch = todo[w] & cm;
-            todo[w] &= ~ch;
-            while (ch) {
-              const int k = w * 64 + __ffsll((long long)ch) - 1;
-              ch &= ch - 1ull;
-              if (in[q] && ((smask[k * NB + blk[q]] >> bit) & 1ull)) {
-                frags++;
-                PS::earlyReject(__int_as_float(0x7f800000), st[q]);  // counts the rejected fragment
-              }
-            }
-          }
-        }
         if (!in[q]) continue;
         const int pix = (py[q] - oy) * TILE + (px[q] - ox);
 #pragma unroll

@@ -92,7 +92,7 @@ class Context:
         return int(v.value)
 
     def set_tile_split(self, on=True):
-        """Heavy 16-px tiles rasterized as four 8 x 8 quadrant CTAs (the default) or whole."""
+        """Heavy 16-px tiles rasterized as four 8 x 8 quadrant CTAs, or whole (the default)."""
         self.L.swr_set_tile_split.argtypes = [ctypes.c_void_p, ctypes.c_int]
         self.L.swr_set_tile_split.restype = ctypes.c_int
         _lib.check(self.L.swr_set_tile_split(self.h, int(bool(on))), "set_tile_split")

@@ -10,12 +10,12 @@ def oracle_render(port, scene, threads=0):
     return t.arrays(), st
 
 
-def gpu_render(scene, tile=16, split=True):
+def gpu_render(scene, tile=16, split=False):
     """tile: 8, 16 or 32 (swr_set_tile_size); split: heavy 16-px tiles as quadrant CTAs."""
     from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
     ds = DeviceScene(scene, tile=tile)
-    if not split:
-        ds.rast.ctx.set_tile_split(False)
+    if split:
+        ds.rast.ctx.set_tile_split(True)
     tg = DeviceTarget(scene)
     st = ds.draw(tg)
     return tg.to_host(), st

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 TRI_SEEDS = list(range(0, 160))
 
 
-def _check(port, sc, tile=16, split=True):
+def _check(port, sc, tile=16, split=False):
     ref, rst = oracle_render(port, sc)
     got, gst = gpu_render(sc, tile=tile, split=split)
     bad = diff(ref, got)
@@ -48,10 +48,10 @@ def test_random_triangles_tile8(gpu_lib, port, seed):
     _check(port, sc, tile=8)
 
 
-@pytest.mark.parametrize("tile,split", [(8, True), (16, False), (32, True)])
+@pytest.mark.parametrize("tile,split", [(8, False), (16, True), (32, False)])
 def test_heavy_tiles_split_or_whole(gpu_lib, port, tile, split):
     """The dense mesh's silhouette tiles (hundreds of bin entries) and the dense soup: by
-    quadrant CTAs (tile 8, and tile 16's default heavy-tile split) and whole."""
+    quadrant CTAs (tile 8; tile 16 with the heavy-tile split) and whole (tile 32)."""
     _check(port, scenes.sphere_scene(8), tile=tile, split=split)
     sc = scenes.soup_scene(1 << 14, width=320, height=240, seed=12, raster=RasterMode.Adaptive)
     _check(port, sc, tile=tile, split=split)
