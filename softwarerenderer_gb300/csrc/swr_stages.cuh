@@ -828,29 +828,74 @@ __global__ void __launch_bounds__(256) k_fill_bins(const uint32_t* status, uint3
   const uint32_t tb0 = T0.tile_base;
   const int tw0 = T0.tiles_x;
   const int tshift = __ffs(tile) - 1;  // tiles are 16 or 32 pixels; pixel boxes are >= 0
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  // one warp per 32 consecutive primitives (the loop is uniform per warp)
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; p0 < np; p0 += stride) {
+    const uint32_t p = p0 + (uint32_t)lane;
     // record words 0-5: flags (0: no tile, as tile_count), draw, pixel box (two float4
     // reads of the 16-byte aligned record)
-    const float4 q0 = __ldg((const float4*)(recs + (size_t)p * RL::R));
-    const float4 q1 = __ldg((const float4*)(recs + (size_t)p * RL::R) + 1);
-    if (!__float_as_int(q0.x)) continue;
-    const int d = __float_as_int(q0.y);
+    int tx0 = 0, ty0 = 0, nx = 1, cnt = 0;
     uint32_t tbase = tb0;
     int tiles_x = tw0;
-    if (d != 0) {
-      const SwrTargetDesc& T = targets[draws[d].target];
-      tbase = T.tile_base;
-      tiles_x = T.tiles_x;
-    }
-    const int tx0 = __float_as_int(q0.z) >> tshift, ty0 = __float_as_int(q0.w) >> tshift;
-    const int tx1 = __float_as_int(q1.x) >> tshift, ty1 = __float_as_int(q1.y) >> tshift;
-    const uint32_t seg = p >> seg_shift;
-    for (int ty = ty0; ty <= ty1; ++ty)
-      for (int tx = tx0; tx <= tx1; ++tx) {
-        const uint32_t cell = (tbase + (uint32_t)(ty * tiles_x + tx)) * SWR_SEGS + seg;
-        const uint32_t pos = atomicSub(&cell_count[cell], 1u) - 1u;
-        bin[cell_start[cell] + pos] = p;
+    if (p < np) {
+      const float4 q0 = __ldg((const float4*)(recs + (size_t)p * RL::R));
+      const float4 q1 = __ldg((const float4*)(recs + (size_t)p * RL::R) + 1);
+      if (__float_as_int(q0.x)) {
+        const int d = __float_as_int(q0.y);
+        if (d != 0) {
+          const SwrTargetDesc& T = targets[draws[d].target];
+          tbase = T.tile_base;
+          tiles_x = T.tiles_x;
+        }
+        tx0 = __float_as_int(q0.z) >> tshift;
+        ty0 = __float_as_int(q0.w) >> tshift;
+        nx = (__float_as_int(q1.x) >> tshift) - tx0 + 1;
+        cnt = nx * ((__float_as_int(q1.y) >> tshift) - ty0 + 1);
       }
+    }
+    const uint32_t seg = p >> seg_shift;
+    auto put = [&](uint32_t prim, uint32_t pseg, uint32_t tb, int tw, int tx, int ty) {
+      const uint32_t cell = (tb + (uint32_t)(ty * tw + tx)) * SWR_SEGS + pseg;
+      const uint32_t pos = atomicSub(&cell_count[cell], 1u) - 1u;
+      bin[cell_start[cell] + pos] = prim;
+    };
+    if (__reduce_max_sync(0xffffffffu, (uint32_t)cnt) <= 2u) {
+      // small primitives (the common case): every lane its own tiles
+      for (int i = 0; i < cnt; ++i) put(p, seg, tbase, tiles_x, tx0 + (i < nx ? i : i - nx), ty0 + (i < nx ? 0 : 1));
+      continue;
+    }
+    // some primitive spans more tiles: the warp's (primitive, tile) pairs are spread over its
+    // lanes, 32 at a time, so one large primitive does not serialise the warp
+    int inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    for (int base = 0; base < total; base += 32) {
+      const int j = base + lane;
+      // owner: the number of lanes whose inclusive count is <= j
+      int src = 0;
+#pragma unroll
+      for (int step = 16; step; step >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, inc, src + step - 1);
+        if (v <= j) src += step;
+      }
+      src = src < 31 ? src : 31;
+      const int first = __shfl_sync(0xffffffffu, inc - cnt, src);
+      const int onx = __shfl_sync(0xffffffffu, nx, src);
+      const int otx0 = __shfl_sync(0xffffffffu, tx0, src);
+      const int oty0 = __shfl_sync(0xffffffffu, ty0, src);
+      const uint32_t otb = __shfl_sync(0xffffffffu, tbase, src);
+      const int otw = __shfl_sync(0xffffffffu, tiles_x, src);
+      if (j < total) {
+        const int local = j - first;
+        const int ry = local / onx;
+        put(p0 + (uint32_t)src, (p0 + (uint32_t)src) >> seg_shift, otb, otw, otx0 + (local - ry * onx), oty0 + ry);
+      }
+    }
   }
 }
 
