@@ -419,7 +419,7 @@ def run_batched(torch, n=256, steps=10):
     scs = scenes.batch_scenes(n)
     best = autotune.tune(scs)
     br = BatchRenderer(scs, tile=best["tile"], graph=best["graph"], pooled=True)
-    autotune.apply_capacity(br, best["capacity"], (best["need"]["primitives"], best["need"]["bin_entries"]))
+    autotune.apply_config(br, best)
     res = {"n_views": n, "triangles_per_step": int(sum(len(x.indices) // 3 for x in scs)),
            "pixels_per_step": int(sum(x.width * x.height for x in scs)), "autotune": best}
     for mode in ("batch", "loop"):

@@ -173,6 +173,11 @@ SWR_API int swr_memory_used(swr_context* ctx, uint64_t* bytes);
  * measured workloads). */
 SWR_API int swr_set_tile_size(swr_context* ctx, int tile);
 SWR_API int swr_set_tile_split(swr_context* ctx, int on);
+/* Persistent geometry front end (no reference counterpart): triangle draws and batches run
+ * vertex shading and triangle assembly as one cooperative launch whose CTAs stay resident
+ * and meet at grid barriers between the stages, instead of three kernels.  Off by default;
+ * a barrier that waits past its limit makes swr_finish return SWR_ECUDA. */
+SWR_API int swr_set_persistent_geometry(swr_context* ctx, int on);
 SWR_API const char* swr_status_string(int status);
 
 /* Tracing (no reference counterpart; the reference has only Benchmark.cpp's chrono).

@@ -13,6 +13,8 @@ Axes (the full product is timed and reported in `tried`):
               "2x"     pre-sized to twice that
             The primitive queue's size also sets the primitive segments of the binning
             (a segment spans capacity / 32 primitive ids), so it changes the sort work.
+  geometry  the best of the above once more with vertex shading and assembly as one
+            persistent cooperative launch ("persistent") instead of three kernels ("kernels")
 """
 import hashlib
 import json
@@ -66,6 +68,12 @@ def needed_capacity(br):
     return int(st["primitives"]), int(st["bin_pairs"])
 
 
+def apply_config(br, best):
+    """Configure a renderer built with best["tile"] / best["graph"] as tuned."""
+    apply_capacity(br, best["capacity"], (best["need"]["primitives"], best["need"]["bin_entries"]))
+    br.ctx.set_persistent_geometry(best.get("geometry") == "persistent")
+
+
 def apply_capacity(br, capacity, need):
     """Configure a renderer's queues for one `capacity` setting (see the module doc)."""
     prims, pairs = need
@@ -96,6 +104,16 @@ def tune(scenes, reps=3, force=False):
                 ms = _time(br, reps)
                 results.append((ms, {"tile": tile, "graph": graph, "capacity": capacity}))
         del br
+    for _, c in results:
+        c["geometry"] = "kernels"
+    # the best configuration once more with the persistent geometry front end (vertex
+    # shading and assembly as one cooperative launch instead of three kernels)
+    ms, best = min(results, key=lambda r: r[0])
+    br = BatchRenderer(scenes, tile=best["tile"], graph=best["graph"], pooled=True)
+    apply_capacity(br, best["capacity"], need)
+    br.ctx.set_persistent_geometry(True)
+    results.append((_time(br, reps), dict(best, geometry="persistent")))
+    del br
     ms, best = min(results, key=lambda r: r[0])
     entry = dict(best, ms=round(ms, 4), need={"primitives": need[0], "bin_entries": need[1]},
                  tried=[dict(c, ms=round(t, 4)) for t, c in results])

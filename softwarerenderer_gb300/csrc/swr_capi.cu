@@ -135,6 +135,8 @@ struct swr_context {
   swr::Buffer big_cells;  // k_sort_cells -> k_sort_big: [count, cell ids...]
   swr::Buffer quad_flag, quad_tiles, quad_count;  // heavy 16-px tiles rasterized as four quadrant CTAs
   int quad_mode = 0;  // 0: off, 1: heavy tiles (more than kQuadMin entries), 2: every tile (8-px raster tiles)
+  bool persistent_geometry = false;  // swr_set_persistent_geometry
+  swr::Buffer geo_bar;                // its grid barrier's two words
   swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
   int slices = 1;           // slices the buffer holds for the current tile count
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
@@ -174,7 +176,7 @@ struct swr_context {
                           &clip_table, &clip_slot, &tri_flags, &batch_counts, &batch_base, &tris, &recs,
                           &tile_count, &pair_off, &keys0, &vals0, &keys1, &vals1, &tile_start, &scratch,
                           &status, &direct_keep, &direct_pos, &lp_refs, &cell_count, &cell_start, &draw_pbase,
-                          &big_cells, &slice_state, &quad_flag, &quad_tiles, &quad_count};
+                          &big_cells, &slice_state, &quad_flag, &quad_tiles, &quad_count, &geo_bar};
     for (swr::Buffer* b : all) b->budget = &budget;
   }
 };
@@ -251,6 +253,7 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
   ok &= c->quad_flag.ensure((size_t)ntiles + 16);
   ok &= c->quad_tiles.ensure((size_t)quad_cap(ntiles) * 4 + 16);
   ok &= c->quad_count.ensure(16);
+  ok &= c->geo_bar.ensure(16);
   if (c->big_cells.bytes < ((size_t)ntiles * SWR_SEGS + 2) * 4) {
     ok &= c->big_cells.ensure(((size_t)ntiles * SWR_SEGS + 2) * 4 + 16);
     // the list length and completion counter start at zero (k_sort_big resets them)
@@ -299,6 +302,22 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
     D.prim_src_cap = c->prim_src_cap < 0xffffffffull ? (uint32_t)c->prim_src_cap : 0xffffffffu;
   }
   D.u = c->u;
+}
+
+// The persistent geometry front end (swr_set_persistent_geometry): vertex shading, assembly
+// count and emit as one cooperative launch.  False when it could not be launched; the
+// caller then launches the three kernels.
+bool geometry_front(swr_context* c, const VsOps* vs, const SwrDrawDesc* draws, int ndraws, const uint32_t* vbase,
+                    uint32_t nverts, const AssembleArgs& aa, uint32_t nbatches, cudaStream_t s) {
+  if (!vs->geometry) return false;
+  if (cudaMemsetAsync(c->geo_bar.p, 0, 8, s) != cudaSuccess ||
+      vs->geometry(draws, ndraws, vbase, nverts, c->ptv.as<float>(), aa, nbatches, c->geo_bar.as<uint32_t>(), s) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  c->launches -= 1;  // one launch for the three counted kernels
+  return true;
 }
 
 // Setup, binning and tile raster for the primitives in c->tris (count on the device).
@@ -677,6 +696,12 @@ int swr_set_tile_size(swr_context* c, int tile) {
   return SWR_OK;
 }
 
+int swr_set_persistent_geometry(swr_context* c, int on) {
+  if (!c) return SWR_EINVAL;
+  c->persistent_geometry = on != 0;
+  return SWR_OK;
+}
+
 int swr_set_tile_split(swr_context* c, int on) {
   if (!c) return SWR_EINVAL;
   if (c->quad_mode != 2) c->quad_mode = on ? 1 : 0;
@@ -744,7 +769,9 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   if ((rc = upload_single(c, D, T, s))) return rc;
   uint32_t* st = c->status.as<uint32_t>();
   mark(c, 0, s);
-  vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts, c->ptv.as<float>(), s);
+  // triangles with the persistent geometry front end: vertex shading and assembly in one launch
+  const bool geo = mode == SWR_DRAW_TRIANGLE && c->persistent_geometry && nbatches;
+  if (!geo) vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts, c->ptv.as<float>(), s);
   mark(c, 1, s);
   c->launches += (nverts ? 1 : 0) + (nbatches ? 2 : 0) + (mode == SWR_DRAW_TRIANGLE ? 0 : 1);
   AssembleArgs aa;
@@ -767,8 +794,13 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   aa.cap_prims = c->cap_prims;
   c->use_draw_pbase = false;
   if (mode == SWR_DRAW_TRIANGLE) {
-    vs->assemble_count(aa, nbatches, s);
-    vs->assemble_emit(aa, nbatches, s);  // derives batch bases and the primitive count itself
+    if (!(geo && geometry_front(c, vs, c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(),
+                                (uint32_t)nverts, aa, nbatches, s))) {
+      if (geo) vs->vertex(c->draws.as<SwrDrawDesc>(), 1, c->draw_vbase.as<uint32_t>(), (uint32_t)nverts,
+                          c->ptv.as<float>(), s);
+      vs->assemble_count(aa, nbatches, s);
+      vs->assemble_emit(aa, nbatches, s);  // derives batch bases and the primitive count itself
+    }
   } else {
     vs->assemble_lp_count(aa, nbatches, s);
     swr::launch(k_batch_scan, 1, 1024, 0, s, c->batch_counts.as<uint2>(), nbatches, c->batch_base.as<uint32_t>(), st,
@@ -959,6 +991,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   memcpy(h + o_tb, tbase.data(), 4 * ntg);
   mix((uint64_t)(uintptr_t)vs); mix((uint64_t)(uintptr_t)ps);  // the programs (their kernels)
   mix((uint64_t)c->quad_mode);
+  mix((uint64_t)c->persistent_geometry);
   mix((uint64_t)vs->S); mix((uint64_t)ps->R); mix((uint64_t)c->tile); mix((uint64_t)n);
   mix(c->cap_prims); mix(c->cap_pairs); mix(c->cap_clip_slots); mix(c->cap_clip_verts);
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
@@ -966,7 +999,7 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
                         c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage,
                         c->slice_state.p, (const void*)(uintptr_t)c->slices, c->quad_flag.p, c->quad_tiles.p,
-                        c->quad_count.p};
+                        c->quad_count.p, c->geo_bar.p};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
   if (c->graph_mode && c->gexec && sig == c->gsig) {
     if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;
@@ -1006,7 +1039,8 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   q = q ? q : cuda_err(cudaGetLastError());
   uint32_t* st = c->status.as<uint32_t>();
   mark(c, 0, s);
-  vs->vertex(c->draws.as<SwrDrawDesc>(), n, c->draw_vbase.as<uint32_t>(), (uint32_t)V, c->ptv.as<float>(), s);
+  const bool geo = c->persistent_geometry && B;
+  if (!geo) vs->vertex(c->draws.as<SwrDrawDesc>(), n, c->draw_vbase.as<uint32_t>(), (uint32_t)V, c->ptv.as<float>(), s);
   mark(c, 1, s);
   AssembleArgs aa;
   memset(&aa, 0, sizeof(aa));
@@ -1028,8 +1062,12 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   aa.cap_clip_verts = c->cap_clip_verts;
   aa.cap_prims = c->cap_prims;
   c->use_draw_pbase = true;
-  vs->assemble_count(aa, (uint32_t)B, s);
-  vs->assemble_emit(aa, (uint32_t)B, s);
+  if (!(geo && geometry_front(c, vs, c->draws.as<SwrDrawDesc>(), n, c->draw_vbase.as<uint32_t>(), (uint32_t)V, aa,
+                              (uint32_t)B, s))) {
+    if (geo) vs->vertex(c->draws.as<SwrDrawDesc>(), n, c->draw_vbase.as<uint32_t>(), (uint32_t)V, c->ptv.as<float>(), s);
+    vs->assemble_count(aa, (uint32_t)B, s);
+    vs->assemble_emit(aa, (uint32_t)B, s);
+  }
   mark(c, 2, s);
   c->launches += (V ? 1 : 0) + (B ? 2 : 0);
   if (!q) q = cuda_err(cudaGetLastError());
@@ -1083,6 +1121,7 @@ int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
   cudaMemsetAsync(c->status.p, 0, kStatusWords * 4, s);
   if ((rc = cuda_err(cudaStreamSynchronize(s)))) return rc;
   if (flags & SWR_F_ANY_OVERFLOW) return SWR_EOVERFLOW;
+  if (flags & SWR_F_BARRIER_TIMEOUT) return SWR_ECUDA;
   if (flags & (SWR_F_BAD_INDEX | SWR_F_BAD_GRAD_INPUT)) return SWR_EINDEX;
   if (flags & SWR_F_SRC_OVERFLOW) return SWR_EINVAL;
   return SWR_OK;

@@ -50,6 +50,7 @@ enum SwrStatusFlags {
   SWR_F_CLIP_COMPLEX = 32,   // a clipped polygon exceeded 16 vertices and was dropped
   SWR_F_SRC_OVERFLOW = 64,   // a caller's primitive-source buffer was too small
   SWR_F_BAD_GRAD_INPUT = 128,  // backward: a winner or source id beyond the given counts
+  SWR_F_BARRIER_TIMEOUT = 256,  // a grid barrier of a persistent launch gave up waiting
 };
 #define SWR_F_ANY_OVERFLOW (SWR_F_CLIP_OVERFLOW | SWR_F_PRIM_OVERFLOW | SWR_F_PAIR_OVERFLOW | SWR_F_FRAG_OVERFLOW)
 #define SWR_ST_STICKY 8  // words SWR_ST_STICKY + i keep the largest value word i reached (i = CLIP_SLOTS..FRAGS)

@@ -16,6 +16,10 @@ struct VsOps {
   void (*assemble_emit)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
   void (*assemble_lp_count)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);  // points, lines
   void (*assemble_lp_emit)(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s);
+  // vertex shading + assembly count + emit as one persistent cooperative launch (k_geometry);
+  // bar: two zeroed words of device memory.  Returns a CUDA error (nothing queued on failure).
+  cudaError_t (*geometry)(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase, uint32_t nverts,
+                          float* ptv, const AssembleArgs& a, uint32_t nbatches, uint32_t* bar, cudaStream_t s);
 };
 
 struct PsOps {
@@ -51,7 +55,7 @@ const PsOps* ps_ops(int id);
 // these headers in the caller's unit, so the library checks that both sides agree on the
 // layout of every structure that crosses between them.
 #define SWR_PROGRAM_MAGIC 0x50525753u  // "SWRP"
-#define SWR_PROGRAM_ABI 1u             // bumped with any change to VsOps, PsOps or their argument structs
+#define SWR_PROGRAM_ABI 2u             // bumped with any change to VsOps, PsOps or their argument structs
 #define SWR_PROGRAM_VERTEX 1u
 #define SWR_PROGRAM_PIXEL 2u
 

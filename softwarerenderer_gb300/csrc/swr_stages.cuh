@@ -61,11 +61,11 @@ __device__ __forceinline__ void to_screen(const SwrDrawDesc& D, float x, float y
   sz = swr_add(swr_mul(swr_mul(0.5f, swr_sub(D.df, D.dn)), nz), swr_mul(0.5f, swr_add(D.dn, D.df)));
 }
 
+// Vertex shading of every vertex, grid-stride over the launch's threads.
 template <class VS>
-__global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ draws, int ndraws,
-                                                const uint32_t* __restrict__ draw_vbase,
-                                                uint32_t nverts, float* __restrict__ ptv) {
-  swr_pdl_entry();
+__device__ __forceinline__ void vertex_stage(const SwrDrawDesc* __restrict__ draws, int ndraws,
+                                             const uint32_t* __restrict__ draw_vbase, uint32_t nverts,
+                                             float* __restrict__ ptv) {
   typedef VLayout<VS::AVarCount, VS::PVarCount> L;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nverts; v += gridDim.x * blockDim.x) {
     const int d = ndraws > 1 ? swr_find_le(draw_vbase, ndraws, v) : 0;
@@ -91,6 +91,14 @@ __global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ 
 #pragma unroll
     for (int i = 0; i < L::S / 4; ++i) dst[i] = make_float4(rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]);
   }
+}
+
+template <class VS>
+__global__ void __launch_bounds__(256) k_vertex(const SwrDrawDesc* __restrict__ draws, int ndraws,
+                                                const uint32_t* __restrict__ draw_vbase,
+                                                uint32_t nverts, float* __restrict__ ptv) {
+  swr_pdl_entry();
+  vertex_stage<VS>(draws, ndraws, draw_vbase, nverts, ptv);
 }
 
 // Direct Rasterizer path: RasterizerVertex (x, y, z, w, avar[16], pvar[16]) records are
@@ -306,10 +314,9 @@ __device__ __forceinline__ uint32_t batch_count(const SwrDrawDesc& D, uint32_t p
 // One CTA per half batch (512 triangles, one per thread): clip / cull and count the
 // survivors: batch_counts[h] = (kept input slots, kept extra fan triangles).
 template <int A, int P>
-__global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
-  swr_pdl_entry();
+__device__ __forceinline__ void assemble_count_block(const AssembleArgs& g, uint32_t hb) {
   __shared__ uint32_t tmp[64];
-  const uint32_t hb = blockIdx.x, b = hb >> 1;
+  const uint32_t b = hb >> 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + (hb & 1) * SWR_HALF;
@@ -323,6 +330,12 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
   uint32_t tin, tex;
   swr_block_sum2(ik, ek, tmp, tin, tex);
   if (threadIdx.x == 0) g.batch_counts[hb] = make_uint2(tin, tex);
+}
+
+template <int A, int P>
+__global__ void __launch_bounds__(SWR_HALF) k_assemble_count(AssembleArgs g) {
+  swr_pdl_entry();
+  assemble_count_block<A, P>(g, blockIdx.x);
 }
 
 // Exclusive scan of per-batch totals -> batch bases; primitive total into the status word.
@@ -349,12 +362,11 @@ static __global__ void __launch_bounds__(1024) k_batch_scan(const uint2* counts,
 // batch base is the sum of the totals of the batches before it; the last batch publishes
 // the primitive count (and flags an undersized primitive queue).
 template <int A, int P>
-__global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
-  swr_pdl_entry();
+__device__ __forceinline__ void assemble_emit_block(const AssembleArgs& g, uint32_t hb, uint32_t nhb) {
   __shared__ uint32_t tmp[64];
   __shared__ uint32_t tmps[32];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
-  const uint32_t hb = blockIdx.x, b = hb >> 1, half = hb & 1;
+  const uint32_t b = hb >> 1, half = hb & 1;
   const int d = g.ndraws > 1 ? swr_find_le(g.draw_bbase, g.ndraws, b) : 0;
   const SwrDrawDesc& D = g.draws[d];
   const uint32_t p0 = (b - D.bbase) * SWR_BATCH_PRIMS + half * SWR_HALF;
@@ -397,7 +409,7 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
   const uint32_t ex = swr_block_exscan((keep & 1u) | ((uint32_t)__popc(keep >> 1) << 16), tmps, &tot);
   uint32_t rin = (ex & 0xffffu) + in_base;
   uint32_t rex = (ex >> 16) + ex_base;
-  if (hb == gridDim.x - 1 && threadIdx.x == 0) {
+  if (hb == nhb - 1 && threadIdx.x == 0) {
     g.status[SWR_ST_PRIMS] = base + batch_total;
     if (base + batch_total > g.cap_prims) atomicOr(&g.status[SWR_ST_FLAGS], SWR_F_PRIM_OVERFLOW);
   }
@@ -434,6 +446,65 @@ __global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
         }
       }
     }
+  }
+}
+
+template <int A, int P>
+__global__ void __launch_bounds__(SWR_HALF) k_assemble_emit(AssembleArgs g) {
+  swr_pdl_entry();
+  assemble_emit_block<A, P>(g, blockIdx.x, gridDim.x);
+}
+
+// Grid barrier of a cooperative launch: bar[0] counts arrivals, bar[1] is the generation.
+// The wait is bounded: past its limit the barrier sets SWR_F_BARRIER_TIMEOUT and returns
+// false, and the caller skips the rest of its work (every CTA ends; none waits forever).
+__device__ __forceinline__ bool swr_grid_sync(uint32_t* bar, uint32_t* status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = bar + 1;
+    const uint32_t g0 = *gen;
+    __threadfence();
+    ok = 1;
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);  // reset before the release: the next barrier counts from zero
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint32_t spins = 0;
+      while (*gen == g0) {
+        if (++spins > (1u << 24)) {  // seconds of waiting: give up
+          atomicOr(&status[SWR_ST_FLAGS], SWR_F_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// The geometry front end of a draw or batch in one persistent cooperative launch: vertex
+// shading, then assembly's count and emit over every half batch, the CTAs staying resident
+// and meeting at grid barriers between the stages (512 threads, the assembly's CTA size).
+template <class VS>
+__global__ void __launch_bounds__(SWR_HALF) k_geometry(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase,
+                                                       uint32_t nverts, float* ptv, AssembleArgs g, uint32_t nhb,
+                                                       uint32_t* bar) {
+  swr_pdl_entry();
+  vertex_stage<VS>(draws, ndraws, draw_vbase, nverts, ptv);
+  if (!swr_grid_sync(bar, g.status)) return;
+  for (uint32_t hb = blockIdx.x; hb < nhb; hb += gridDim.x) {
+    assemble_count_block<VS::AVarCount, VS::PVarCount>(g, hb);
+    __syncthreads();  // the block's shared scratch is reused by its next half batch
+  }
+  if (!swr_grid_sync(bar, g.status)) return;
+  for (uint32_t hb = blockIdx.x; hb < nhb; hb += gridDim.x) {
+    assemble_emit_block<VS::AVarCount, VS::PVarCount>(g, hb, nhb);
+    __syncthreads();
   }
 }
 

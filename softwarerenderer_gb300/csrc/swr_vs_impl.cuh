@@ -37,6 +37,34 @@ inline void run_lp_emit(const AssembleArgs& a, uint32_t nbatches, cudaStream_t s
   if (nbatches) swr::launch(k_assemble_lp_emit, nbatches, 256, 0, s, a);
 }
 
+// Persistent geometry front end: as many 512-thread CTAs as can be resident at once (a
+// cooperative launch, so the grid barriers inside cannot wait on CTAs that never start).
+template <class VS>
+cudaError_t run_geometry(const SwrDrawDesc* draws, int ndraws, const uint32_t* draw_vbase, uint32_t nverts, float* ptv,
+                         const AssembleArgs& a, uint32_t nbatches, uint32_t* bar, cudaStream_t s) {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_geometry<VS>, SWR_HALF, 0) != cudaSuccess ||
+        per_sm < 1)
+      return cudaErrorLaunchFailure;
+    grid = sms * per_sm;
+  }
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(SWR_HALF);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_geometry<VS>, draws, ndraws, draw_vbase, nverts, ptv, a, 2 * nbatches, bar);
+}
+
 template <class VS>
 VsOps make_vs() {
   VsOps o;
@@ -51,6 +79,7 @@ VsOps make_vs() {
   o.assemble_emit = &run_emit<VS>;
   o.assemble_lp_count = &run_lp_count<VS>;
   o.assemble_lp_emit = &run_lp_emit;
+  o.geometry = &run_geometry<VS>;
   return o;
 }
 

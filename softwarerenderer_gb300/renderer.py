@@ -91,6 +91,12 @@ class Context:
         _lib.check(L.swr_memory_used(self.h, ctypes.byref(v)), "memory_used")
         return int(v.value)
 
+    def set_persistent_geometry(self, on=True):
+        """Vertex shading and triangle assembly as one persistent cooperative launch."""
+        self.L.swr_set_persistent_geometry.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.swr_set_persistent_geometry.restype = ctypes.c_int
+        _lib.check(self.L.swr_set_persistent_geometry(self.h, int(bool(on))), "set_persistent_geometry")
+
     def set_tile_split(self, on=True):
         """Heavy 16-px tiles rasterized as four 8 x 8 quadrant CTAs, or whole (the default)."""
         self.L.swr_set_tile_split.argtypes = [ctypes.c_void_p, ctypes.c_int]

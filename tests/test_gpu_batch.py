@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from softwarerenderer_gb300 import scenes
+from softwarerenderer_gb300.abi import DrawMode
 
 from .parity import diff, oracle_render
 
@@ -104,12 +105,39 @@ def test_autotuner_covers_tile_capacity_graph(gpu_lib, port):
     from softwarerenderer_gb300.batch import BatchRenderer
     scs = _small_batch(6, seed=45)
     best = autotune.tune(scs, reps=1, force=True)
-    combos = {(t["tile"], t["capacity"], t["graph"]) for t in best["tried"]}
+    combos = {(t["tile"], t["capacity"], t["graph"]) for t in best["tried"] if t["geometry"] == "kernels"}
     assert combos == {(t, c, g) for t in autotune.TILES for c in autotune.CAPACITIES for g in autotune.GRAPHS}
+    assert any(t["geometry"] == "persistent" for t in best["tried"])
     br = BatchRenderer(scs, aux=True, tile=best["tile"], graph=best["graph"])
-    autotune.apply_capacity(br, best["capacity"], (best["need"]["primitives"], best["need"]["bin_entries"]))
+    autotune.apply_config(br, best)
     br.clear()
     br.draw()
     for sc, tg in zip(scs, br.targets):
         ref, _ = oracle_render(port, sc)
+        assert not diff(ref, tg.to_host()), sc.name
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_persistent_geometry_matches_oracle(gpu_lib, port, graph):
+    """Vertex shading and assembly as one cooperative launch with grid barriers
+    (swr_set_persistent_geometry): a batch of meshes (captured and replayed) and single
+    draws with near-plane clipping and several 1024-triangle batches render exactly."""
+    from softwarerenderer_gb300.batch import BatchRenderer
+    from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
+    scs = _small_batch(8, seed=47)
+    br = BatchRenderer(scs, aux=True, graph=graph)
+    br.ctx.set_persistent_geometry(True)
+    for rep in range(2):
+        br.clear()
+        br.draw()
+        for sc, tg in zip(scs, br.targets):
+            ref, _ = oracle_render(port, sc)
+            assert not diff(ref, tg.to_host()), (rep, sc.name)
+    for sc in (scenes.sphere_scene(29), scenes.random_scene(5001, direct=False, draw_mode=DrawMode.Triangle, n_prims=3000)):
+        ds = DeviceScene(sc)
+        ds.rast.ctx.set_persistent_geometry(True)
+        tg = DeviceTarget(sc)
+        st = ds.draw(tg)
+        ref, rst = oracle_render(port, sc)
+        assert st["fragments"] == rst["fragments"]
         assert not diff(ref, tg.to_host()), sc.name
