@@ -20,7 +20,7 @@
 #define SWR_SLICES_MAX 8          // overwrite shaders: CTAs (ordered bin slices) per tile of more than
                                   // SWR_RASTER_SORT entries, merged by k_merge_slices
 #ifndef SWR_PIX_WALK
-#define SWR_PIX_WALK 1            // k_raster's per-pixel primitive walk (all but the overwrite shaders)
+#define SWR_PIX_WALK 1            // k_raster's per-pixel primitive walk (shaders without depth cull or overwrite)
 #endif
 #ifndef SWR_DEPTH_CULL
 #define SWR_DEPTH_CULL 1          // k_raster's per-chunk tile depth cull (depth-tested shaders)

@@ -1375,7 +1375,9 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   // the set of compacted primitives covering it (set in C1), so in C2 every lane visits only
   // its own pixel's primitives instead of all primitives touching its warp's half block.
   constexpr int HW = (CH + 63) / 64;  // 64-primitive words of a chunk
-  constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !SwrOverwrite<PS>::value;
+  // (Not for the depth-culling shaders: measured on the 4K soup, whose chunks mix compacted
+  // small primitives with large ones, the per-lane loops cost 30 % more raster time.)
+  constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !kCull && !SwrOverwrite<PS>::value;
   __shared__ uint64_t spm[kPixWalk ? TILE * TILE * HW : 1];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1802,9 +1804,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
       const int half = (py[q] >> 2) & 1;
-      // Chunks whose depth cull is on compact nothing: every primitive then goes through the
-      // warp-uniform walk below, which costs less than per-lane loops over the same list.
-      if (kPixWalk && !(kCull && scull_on)) {
+      if constexpr (kPixWalk) {
         // the warp's primitives that were not compacted and touch its half block (ballot),
         // plus this pixel's compacted primitives; visited per lane in increasing order
         uint64_t todo[HW];
