@@ -39,9 +39,15 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
             "test, 32 seeded poses (3 near-plane clipped), 1 frame per step")
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one headline k_raster launch (an ncu --set full
-# capture of the first timed frame's raster launch of this bench's headline section)
+# From ncu captures of one headline k_raster launch (profiles/k_raster_lambert_sphere7_1080p.md):
+# dram__bytes_read.sum + dram__bytes_write.sum with the L2 as the frame's earlier kernels
+# leave it (--cache-control none: the setup records and the cleared target are still in L2)
+# and with the L2 flushed before the launch (ncu's default), and smsp__inst_executed.sum
+# (warp instructions) per drawPixel call of that frame.
 NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 21398784}
+NCU_DRAM_BYTES_COLD = {"raster": 21398784}
+NCU_WARP_INST_PER_FRAGMENT = {"raster": None}
+SMS = 152
 
 
 def peaks():
@@ -364,7 +370,9 @@ def main():
                 "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 5), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                "traffic": traffic, "traffic_l2_flushed": NCU_DRAM_BYTES_COLD.get(dom) if args.tile == 16 else None,
+                "traffic_over_algorithmic": round(traffic / alg, 3) if traffic and alg else None,
+                "algorithmic_bytes_per_launch": alg,
                 "launch_ms": round(stages[dom] / args.steps, 4)}
     fb = frame_bytes(n_idx, vbytes, pixels, frags / args.steps, passes / args.steps)
     frame_roof = {"bytes_per_frame": fb, "achieved_gbs": round(fb / (ms / args.steps / 1e3) / 1e9, 2),
@@ -387,6 +395,19 @@ def main():
             cb = cpu_baseline()
         except Exception as ex:  # pragma: no cover
             cb = {"error": str(ex)}
+    # issue roofline of the same kernel: its warp instructions (ncu, per fragment, times this
+    # run's fragments per frame) over what 152 SMs x 4 schedulers issue at the sampled clock
+    clocks = clk.summary()
+    ipf = NCU_WARP_INST_PER_FRAGMENT.get(dom)
+    issue_roof = None
+    if ipf and clocks.get("sm_mhz") and args.tile == 16:
+        inst = ipf * frags / args.steps
+        rate = SMS * 4 * clocks["sm_mhz"] * 1e6
+        ideal_ms = inst / rate * 1e3
+        issue_roof = {"bound": "issue", "kernel": roofline["kernel"], "warp_inst_per_fragment": ipf,
+                      "warp_inst_per_launch": round(inst), "issue_slots_per_s": rate,
+                      "ideal_ms": round(ideal_ms, 4), "launch_ms": roofline["launch_ms"],
+                      "frac": round(ideal_ms / roofline["launch_ms"], 4) if roofline["launch_ms"] else None}
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 4), "unit": "Gfrags/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
@@ -400,8 +421,8 @@ def main():
                 "stage_ms_per_frame": {k: round(v / args.steps, 4) for k, v in stages.items()},
                 "stage_pass_ms_per_frame": round(ps0.elapsed_time(ps1) / args.steps, 4),
                 "gpu_launches": int(st["launches"]),
-                "roofline": roofline, "frame_roofline": frame_roof,
-                "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cb, "batched": batched,
+                "roofline": roofline, "issue_roofline": issue_roof, "frame_roofline": frame_roof,
+                "clocks": clocks, "e2e": e2e, "cpu_baseline": cb, "batched": batched,
                 "differentiable": diffr, "benchmark_program": bprog, "soup_4k": soup}
         print(json.dumps(line))
     if dist:
@@ -570,6 +591,15 @@ def run_diff(torch, steps=20, warmup=3):
     res["fwd_bwd_views_per_s"] = round(P.n_views / (res["fwd_bwd_ms"] / 1e3), 1)
     res["fwd_bwd_over_fwd"] = round(res["fwd_bwd_ms"] / res["fwd_ms"], 3)
     res["covered_pixels"] = int((dr.winner >= 0).sum())
+    # how the gradients are checked (tests/test_gpu_diff.py, tests/test_diff_oracle.py)
+    res["gradient_checks"] = {
+        "vs_cpu_reference": "all parameters, relative 2-norm error <= 1e-3 per group (rgb, uv, position, texels)",
+        "vs_central_fd_h1e-3": "vertex rgb, uv and texels: plain central differences at h = 1e-3, 256 "
+                               "sampled parameters per group, within 1e-3",
+        "positions": "plain central FD at h = 1e-3 meets 1e-3 only on a coarser mesh (icosphere-4, 27-px "
+                     "triangles: 6e-4); on this level-6 mesh (1.7-px triangles) its O(h^2) curvature term "
+                     "leaves ~7e-3, so positions are checked against Richardson-extrapolated differences "
+                     "(h and h/2; 4e-5) on vertices whose visible triangles have >= 1 px altitude"}
     return res
 
 
