@@ -39,14 +39,15 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
             "test, 32 seeded poses (3 near-plane clipped), 1 frame per step")
 
 
-# From ncu captures of one headline k_raster launch (profiles/k_raster_lambert_sphere7_1080p.md):
+# Means over the headline k_raster launches of the 32 timed poses, from ncu captures of
+# `python bench.py --steps 32 --warmup 3 --no-...` (profiles/k_raster_lambert_sphere7_1080p.md):
 # dram__bytes_read.sum + dram__bytes_write.sum with the L2 as the frame's earlier kernels
 # leave it (--cache-control none: the setup records and the cleared target are still in L2)
-# and with the L2 flushed before the launch (ncu's default), and smsp__inst_executed.sum
-# (warp instructions) per drawPixel call of that frame.
-NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 21398784}
-NCU_DRAM_BYTES_COLD = {"raster": 21398784}
-NCU_WARP_INST_PER_FRAGMENT = {"raster": None}
+# and with the L2 flushed before every launch (ncu's default), and smsp__inst_executed.sum
+# (warp instructions) per launch.
+NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 8438616}
+NCU_DRAM_BYTES_COLD = {"raster": 19721760}
+NCU_WARP_INST_PER_LAUNCH = {"raster": 38681102}
 SMS = 152
 
 
@@ -395,17 +396,17 @@ def main():
             cb = cpu_baseline()
         except Exception as ex:  # pragma: no cover
             cb = {"error": str(ex)}
-    # issue roofline of the same kernel: its warp instructions (ncu, per fragment, times this
-    # run's fragments per frame) over what 152 SMs x 4 schedulers issue at the sampled clock
+    # issue roofline of the same kernel: its warp instructions per launch (ncu, mean over the
+    # 32 poses) over what 152 SMs x 4 schedulers issue at the clock sampled during the frames
     clocks = clk.summary()
-    ipf = NCU_WARP_INST_PER_FRAGMENT.get(dom)
+    inst = NCU_WARP_INST_PER_LAUNCH.get(dom)
     issue_roof = None
-    if ipf and clocks.get("sm_mhz") and args.tile == 16:
-        inst = ipf * frags / args.steps
+    if inst and clocks.get("sm_mhz") and args.tile == 16:
         rate = SMS * 4 * clocks["sm_mhz"] * 1e6
         ideal_ms = inst / rate * 1e3
-        issue_roof = {"bound": "issue", "kernel": roofline["kernel"], "warp_inst_per_fragment": ipf,
-                      "warp_inst_per_launch": round(inst), "issue_slots_per_s": rate,
+        issue_roof = {"bound": "issue", "kernel": roofline["kernel"],
+                      "warp_inst_per_fragment": round(inst / (frags / args.steps), 2),
+                      "warp_inst_per_launch": inst, "issue_slots_per_s": rate,
                       "ideal_ms": round(ideal_ms, 4), "launch_ms": roofline["launch_ms"],
                       "frac": round(ideal_ms / roofline["launch_ms"], 4) if roofline["launch_ms"] else None}
     if rank == 0:
