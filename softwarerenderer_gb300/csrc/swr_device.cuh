@@ -10,9 +10,6 @@
 #define SWR_BLOCK 8           // swr::BlockSize (IRasterizer.h:33)
 #define SWR_CLIP_REF 0x80000000u  // vertex references with this bit address the clip-vertex buffer
 #define SWR_SEGS 32               // primitive segments of the binning (cells per tile)
-#ifndef SWR_CHUNK
-#define SWR_CHUNK 64              // binned primitives the tile raster stages per chunk
-#endif
 #ifndef SWR_RASTER_MINB
 #define SWR_RASTER_MINB 0         // k_raster CTAs per SM to plan registers for (0: per shader)
 #endif

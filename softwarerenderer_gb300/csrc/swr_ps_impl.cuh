@@ -8,7 +8,6 @@ namespace swr {
 namespace {
 
 constexpr int kGrid = 152 * 8;
-constexpr int kChunk = SWR_CHUNK;  // primitives staged in shared memory per bin chunk
 
 template <class PS>
 void run_direct(const float* rv, uint32_t n, float* ptv, cudaStream_t s) {
@@ -43,6 +42,7 @@ void run_fill(const uint32_t* status, uint32_t cap_prims, const float* recs,
 
 template <class PS>
 void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) {
+  constexpr int kChunk = SwrRasterChunk<PS>::value;  // primitives staged in shared memory per bin chunk
   if (!ntiles) return;
   // one CTA per tile, or per (tile, slice) for sliced overwrite shaders; Block-only
   // submissions run the instantiation without the Span-mode passes
