@@ -146,7 +146,9 @@ class DummyVertexShader : public VertexShaderBase<DummyVertexShader> {};
 
 // PixelShaderBase.h:40-137.  Derive, redefine the flags and counts and drawPixel
 // (__device__).  An optional `static const int RasterOccupancy` (1-8, default 4) sets how
-// many 256-thread tile rasterizer blocks per SM the shader's register use must allow.
+// many 256-thread tile rasterizer blocks per SM the shader's register use must allow, and
+// an optional `static const int RasterChunk` (32, 64, 96 or 128, default 64) how many
+// binned primitives the tile rasterizer stages at a time.
 template <class Derived>
 class PixelShaderBase {
  public:
@@ -209,7 +211,7 @@ template <class PS>
 struct UserPS {
   enum { AVarCount = PS::AVarCount, PVarCount = PS::PVarCount, InterpolateZ = PS::InterpolateZ ? 1 : 0,
          InterpolateW = PS::InterpolateW ? 1 : 0, HasDepth = 0, NoCompact = 1,
-         RasterOccupancy = SwrRasterOccupancy<PS>::value };
+         RasterOccupancy = SwrRasterOccupancy<PS>::value, RasterChunk = SwrRasterChunk<PS>::value };
   static_assert(PS::AVarCount >= 0 && PS::AVarCount <= MaxAVars, "AVarCount <= MaxAVars");
   static_assert(PS::PVarCount >= 0 && PS::PVarCount <= MaxPVars, "PVarCount <= MaxPVars");
   struct State {
