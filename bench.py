@@ -45,9 +45,9 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
 # leave it (--cache-control none: the setup records and the cleared target are still in L2)
 # and with the L2 flushed before every launch (ncu's default), and smsp__inst_executed.sum
 # (warp instructions) per launch.
-NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 8438616}
-NCU_DRAM_BYTES_COLD = {"raster": 19721760}
-NCU_WARP_INST_PER_LAUNCH = {"raster": 38681102}
+NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 4531120}
+NCU_DRAM_BYTES_COLD = {"raster": 19736520}
+NCU_WARP_INST_PER_LAUNCH = {"raster": 38414947}
 SMS = 152
 
 
