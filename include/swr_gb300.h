@@ -178,6 +178,11 @@ SWR_API int swr_set_tile_split(swr_context* ctx, int on);
  * and meet at grid barriers between the stages, instead of three kernels.  Off by default;
  * a barrier that waits past its limit makes swr_finish return SWR_ECUDA. */
 SWR_API int swr_set_persistent_geometry(swr_context* ctx, int on);
+/* Test hook of that bounded wait: while on, the persistent launch's grid barrier starts from
+ * an arrival count no arrival can complete, so every CTA waits out its limit (about a
+ * second), gives up and ends; the draw leaves its targets untouched and swr_finish returns
+ * SWR_ECUDA.  The context stays usable. */
+SWR_API int swr_test_stall_geometry_barrier(swr_context* ctx, int on);
 SWR_API const char* swr_status_string(int status);
 
 /* Tracing (no reference counterpart; the reference has only Benchmark.cpp's chrono).

@@ -136,6 +136,7 @@ struct swr_context {
   swr::Buffer quad_flag, quad_tiles, quad_count;  // heavy 16-px tiles rasterized as four quadrant CTAs
   int quad_mode = 0;  // 0: off, 1: heavy tiles (more than kQuadMin entries), 2: every tile (8-px raster tiles)
   bool persistent_geometry = false;  // swr_set_persistent_geometry
+  bool geo_stall = false;             // swr_test_stall_geometry_barrier
   swr::Buffer geo_bar;                // its grid barrier's two words
   swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
   int slices = 1;           // slices the buffer holds for the current tile count
@@ -310,7 +311,9 @@ void fill_draw(const swr_context* c, SwrDrawDesc& D, int mode) {
 bool geometry_front(swr_context* c, const VsOps* vs, const SwrDrawDesc* draws, int ndraws, const uint32_t* vbase,
                     uint32_t nverts, const AssembleArgs& aa, uint32_t nbatches, cudaStream_t s) {
   if (!vs->geometry) return false;
-  if (cudaMemsetAsync(c->geo_bar.p, 0, 8, s) != cudaSuccess ||
+  // (the test hook starts the arrival count where no arrival can complete the barrier)
+  if (cudaMemsetAsync(c->geo_bar.p, c->geo_stall ? 0x40 : 0, 4, s) != cudaSuccess ||
+      cudaMemsetAsync(c->geo_bar.as<uint32_t>() + 1, 0, 4, s) != cudaSuccess ||
       vs->geometry(draws, ndraws, vbase, nverts, c->ptv.as<float>(), aa, nbatches, c->geo_bar.as<uint32_t>(), s) !=
           cudaSuccess) {
     cudaGetLastError();
@@ -699,6 +702,12 @@ int swr_set_tile_size(swr_context* c, int tile) {
 int swr_set_persistent_geometry(swr_context* c, int on) {
   if (!c) return SWR_EINVAL;
   c->persistent_geometry = on != 0;
+  return SWR_OK;
+}
+
+int swr_test_stall_geometry_barrier(swr_context* c, int on) {
+  if (!c) return SWR_EINVAL;
+  c->geo_stall = on != 0;
   return SWR_OK;
 }
 

@@ -243,7 +243,7 @@ struct PsTexNearest {
 struct PsLambert {
   // 128-primitive chunks: on the dense 1080p mesh 2 % faster than 64 (fewer chunk passes in
   // the silhouette tiles that set the raster's length); 64 suits the other workloads
-  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 6,
+  enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5,
          DepthCull = 0, RasterChunk = 128 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }

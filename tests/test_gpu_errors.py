@@ -116,3 +116,33 @@ def test_memory_limit_returns_enomem_and_queues_nothing(gpu_lib, port):
     assert st["fragments"] == rst["fragments"]
     assert not diff(ref, tg.to_host())
     assert ctx.memory_used() > held + 64 * 1024
+
+
+def test_persistent_geometry_barrier_wait_runs_out(gpu_lib, port):
+    """The persistent geometry launch's grid barriers wait a bounded time: started from an
+    arrival count that can never complete (a test hook, no GPU fault), every CTA gives up
+    after about a second and the draw reports SWR_ECUDA with its target untouched; the same
+    context then draws exactly."""
+    import ctypes
+    from softwarerenderer_gb300 import _lib
+    from softwarerenderer_gb300.device import DeviceScene
+    sc = _scene()
+    ds = DeviceScene(sc)
+    ctx = ds.rast.ctx
+    ctx.set_persistent_geometry(True)
+    ctx.L.swr_test_stall_geometry_barrier.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    ctx.L.swr_test_stall_geometry_barrier.restype = ctypes.c_int
+    assert ctx.L.swr_test_stall_geometry_barrier(ctx.h, 1) == 0
+    tg = _target(sc)
+    before = tg.to_host()
+    ds.draw(tg, sync=False)
+    rc, st = ctx.finish()
+    assert rc == _lib.SWR_ECUDA, rc
+    assert st["flags"] & 256  # SWR_F_BARRIER_TIMEOUT
+    assert st["fragments"] == 0
+    assert not diff(before, tg.to_host())
+    assert ctx.L.swr_test_stall_geometry_barrier(ctx.h, 0) == 0
+    st2 = ds.draw(tg)
+    ref, rst = _oracle(port, sc)
+    assert st2["fragments"] == rst["fragments"]
+    assert not diff(ref, tg.to_host())
