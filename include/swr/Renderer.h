@@ -22,7 +22,8 @@
 //   * Vertex attribute, index and RasterizerVertex arrays may be device memory
 //     (cudaMalloc / cudaMallocManaged; used in place, bounds from the allocation's extent)
 //     or ordinary host memory (copied to the device at every draw: attributes then need
-//     host indices, which give the vertex count).
+//     host indices, which give the vertex count, and each host attribute array must be
+//     readable for (largest index + 1) x stride bytes).
 //   * drawElements and the draw* calls return once the draw has finished on the GPU, like
 //     the reference's; a failure throws swr::Error (the reference asserts).
 //   * The render target is the region [0, scissor x + width) x [0, scissor y + height)
@@ -133,6 +134,10 @@ struct PixelData {
 };
 
 // VertexShaderBase.h:33-51.  Derive, redefine the counts and processVertex (__device__).
+// Vertex v is shaded when a whole stride of each attribute buffer is there at v.  A shader
+// reading a stream interleaved at an offset inside larger records (whose last element ends
+// before a full stride) states with `static const int AttribBytes` how many bytes it reads
+// per element (at least those it reads from that stream).
 template <class Derived>
 class VertexShaderBase {
  public:
@@ -179,10 +184,22 @@ inline void check(int rc, const char* what) {
 }
 
 // The pipeline's vertex-shader contract (k_vertex) over a VertexShaderBase class.
+// Bytes a vertex shader reads from each attribute element: `static const int AttribBytes` in
+// the class, else 0 (a whole stride).  A vertex is shaded only if that many bytes of its
+// element lie inside every attribute buffer.
+template <class VS, class = void>
+struct AttribBytes {
+  enum { value = 0 };
+};
+template <class VS>
+struct AttribBytes<VS, decltype((void)VS::AttribBytes)> {
+  enum { value = VS::AttribBytes };
+};
+
 template <class VS>
 struct UserVS {
-  enum { AttribCount = VS::AttribCount, AVarCount = VS::AVarCount, PVarCount = VS::PVarCount, Bytes0 = 0,
-         Bytes1 = 0 };
+  enum { AttribCount = VS::AttribCount, AVarCount = VS::AVarCount, PVarCount = VS::PVarCount,
+         Bytes0 = AttribBytes<VS>::value, Bytes1 = AttribBytes<VS>::value };
   static_assert(VS::AttribCount >= 0 && VS::AttribCount <= MaxVertexAttribs, "AttribCount <= MaxVertexAttribs");
   static_assert(VS::AVarCount >= 0 && VS::AVarCount <= MaxAVars, "AVarCount <= MaxAVars");
   static_assert(VS::PVarCount >= 0 && VS::PVarCount <= MaxPVars, "PVarCount <= MaxPVars");
