@@ -173,6 +173,15 @@ SWR_API int swr_memory_used(swr_context* ctx, uint64_t* bytes);
  * measured workloads). */
 SWR_API int swr_set_tile_size(swr_context* ctx, int tile);
 SWR_API int swr_set_tile_split(swr_context* ctx, int on);
+/* Heavy-tile slicing (no reference counterpart).  With a built-in depth-tested shader whose
+ * result is the first fragment of smallest depth (Lambert, Lambert-textured, vertex colour,
+ * nearest texture), a tile of more than `chunks` raster chunks of bin entries is rasterized
+ * by four CTAs, each over a run of whole chunks from the draw's starting framebuffer, and
+ * the runs are merged in primitive order: colour, depth, winner and fragment counts are
+ * those of the sequential draw.  Only the `passes` statistic differs: each run counts its
+ * depth-test passes against the depth its run started from.  chunks = 0 turns it off, -1
+ * (the default) takes the shader's own setting (the Lambert shader: 1; the others: off). */
+SWR_API int swr_set_tile_slicing(swr_context* ctx, int chunks);
 /* Persistent geometry front end (no reference counterpart): triangle draws and batches run
  * vertex shading and triangle assembly as one cooperative launch whose CTAs stay resident
  * and meet at grid barriers between the stages, instead of three kernels.  Off by default;

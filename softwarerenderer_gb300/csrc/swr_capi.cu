@@ -33,6 +33,15 @@ uint32_t quad_cap(uint32_t ntiles) {
   return cap < ntiles ? cap : ntiles;
 }
 
+// Tiles k_sort_cells may list for heavy-tile runs (depth-min shaders): every slot adds
+// SWR_DSLICES CTAs at the front of the raster grid, used or not.  On the dense 1080p mesh
+// (about 350 tiles of more than one chunk) 512 slots measured 0.9 % faster than 1020 and
+// 304 slots 7 % slower (heavy tiles left whole).
+uint32_t slice_cap(uint32_t ntiles) {
+  const uint32_t cap = quad_cap(ntiles);
+  return cap < 512 ? cap : 512;
+}
+
 // Descriptor upload from pinned host staging (device-accessible under unified addressing)
 // by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
 // large host<->device copy the application runs on another stream, delaying the draw.
@@ -140,6 +149,10 @@ struct swr_context {
   swr::Buffer geo_bar;                // its grid barrier's two words
   swr::Buffer slice_state;  // overwrite shaders: per (tile, slice, pixel) State of sliced tiles
   int slices = 1;           // slices the buffer holds for the current tile count
+  // depth-min shaders: heavy tiles rasterized in SWR_DSLICES runs (swr_set_tile_slicing)
+  swr::Buffer dslice_state, dslice_done;
+  int dslice_chunks = -1;  // tiles of more than this many raster chunks (-1: the shader's default)
+  bool dslice_ok = false;  // the buffers hold the current tile count's runs
   bool use_draw_pbase = false;  // set while queuing drawElements / batch draws
   int32_t* prim_src = nullptr;  // swr_set_primitive_source
   uint64_t prim_src_cap = 0;
@@ -177,7 +190,8 @@ struct swr_context {
                           &clip_table, &clip_slot, &tri_flags, &batch_counts, &batch_base, &tris, &recs,
                           &tile_count, &pair_off, &keys0, &vals0, &keys1, &vals1, &tile_start, &scratch,
                           &status, &direct_keep, &direct_pos, &lp_refs, &cell_count, &cell_start, &draw_pbase,
-                          &big_cells, &slice_state, &quad_flag, &quad_tiles, &quad_count, &geo_bar};
+                          &big_cells, &slice_state, &quad_flag, &quad_tiles, &quad_count, &geo_bar,
+                          &dslice_state, &dslice_done};
     for (swr::Buffer* b : all) b->budget = &budget;
   }
 };
@@ -268,6 +282,16 @@ int ensure_capacity(swr_context* c, uint32_t nverts_ptv, int S, uint32_t nsub, u
     int k = SWR_SLICES_MAX;
     while (k > 1 && per_slice * (size_t)k > ((size_t)512 << 20)) --k;
     if (k > 1 && c->slice_state.ensure(per_slice * (size_t)k)) c->slices = k;
+  }
+  // Depth-min shaders: the listed heavy tiles' runs (optional, like the slices above; the
+  // per-slot completion counters start at zero and every merge leaves its own at zero)
+  c->dslice_ok = false;
+  if (ps && ps->depth_min && (c->dslice_chunks < 0 ? ps->slice_chunks : c->dslice_chunks) > 0) {
+    const size_t slots = slice_cap(ntiles);
+    bool d = c->dslice_state.ensure(slots * SWR_DSLICES * c->tile * c->tile * (size_t)ps->state_bytes + 16);
+    if (d && c->dslice_done.bytes < slots * 4 + 16)
+      d = c->dslice_done.ensure(slots * 4 + 16) && cudaMemset(c->dslice_done.p, 0, c->dslice_done.bytes) == cudaSuccess;
+    c->dslice_ok = d;
   }
   const size_t sw = sort_scratch_words(c->cap_pairs) + scan_scratch_words(c->cap_prims) + 64 + 2 * scan_scratch_words(ntiles * SWR_SEGS);
   ok &= c->scratch.ensure(sw * 4);
@@ -369,15 +393,20 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   // is allocated and reset by k_sort_big's last block, which also closes the draw)
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
-  // heavy-tile quadrant CTAs (16-px tiles, shaders other than the overwrite ones)
-  const bool quads = c->tile == 16 && !ps->overwrite && c->quad_mode != 0;
+  // heavy tiles listed by k_sort_cells: rasterized in runs of chunks (depth-min shaders,
+  // tiles of more than one chunk), or else as quadrant CTAs (16-px tiles, shaders other
+  // than the overwrite ones; 8-px raster tiles split every tile)
+  const int slice_chunks = c->dslice_chunks < 0 ? ps->slice_chunks : c->dslice_chunks;
+  const bool dsl = ps->depth_min && slice_chunks > 0 && c->dslice_ok && c->quad_mode != 2;
+  const bool quads = !dsl && c->tile == 16 && !ps->overwrite && c->quad_mode != 0;
   const bool quad_list = quads && c->quad_mode == 1;
-  const uint32_t qcap = quad_cap(ntiles);
-  if (quad_list) cudaMemsetAsync(c->quad_count.p, 0, 4, s);
+  const bool listed = dsl || quad_list;
+  const uint32_t qcap = dsl ? slice_cap(ntiles) : quad_cap(ntiles);
+  if (listed) cudaMemsetAsync(c->quad_count.p, 0, 4, s);
   swr::launch(k_sort_cells, (ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s, st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
       big, (uint32_t)SWR_RASTER_SORT,
-      quad_list ? c->quad_flag.as<uint8_t>() : nullptr, c->quad_tiles.as<uint32_t>(), c->quad_count.as<uint32_t>(), qcap,
-      kQuadMin);
+      listed ? c->quad_flag.as<uint8_t>() : nullptr, c->quad_tiles.as<uint32_t>(), c->quad_count.as<uint32_t>(), qcap,
+      dsl ? (uint32_t)(slice_chunks * ps->chunk) : kQuadMin);
   if (use_big) {
     swr::launch(k_sort_big, kBigSortWarps / big_warps, 32 * big_warps, bm_bytes * big_warps, s, st, cstart, ncells, c->cap_pairs, seg_shift, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), big + 2, big);
     c->launches += 1;
@@ -400,11 +429,14 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   ra.has_span = has_span ? 1 : 0;
   ra.slices = ps->overwrite ? c->slices : 1;
   ra.slice_state = c->slice_state.p;
-  ra.quad_flag = quad_list ? c->quad_flag.as<uint8_t>() : nullptr;
+  ra.quad_flag = listed ? c->quad_flag.as<uint8_t>() : nullptr;
   ra.quad_tiles = c->quad_tiles.as<uint32_t>();
   ra.quad_count = c->quad_count.as<uint32_t>();
   ra.quad_cap = qcap;
   ra.quad_all = quads && c->quad_mode == 2;
+  ra.dslice = dsl ? 1 : 0;
+  ra.dslice_state = c->dslice_state.p;
+  ra.dslice_done = c->dslice_done.as<uint32_t>();
   ps->raster(ra, ntiles, c->tile, s);
   if (ra.slices > 1) c->launches += 1;  // k_merge_slices
   mark(c, 5, s);
@@ -717,6 +749,12 @@ int swr_set_tile_split(swr_context* c, int on) {
   return SWR_OK;
 }
 
+int swr_set_tile_slicing(swr_context* c, int chunks) {
+  if (!c || chunks < -1) return SWR_EINVAL;
+  c->dslice_chunks = chunks;
+  return SWR_OK;
+}
+
 int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* indices, void* stream) {
   if (!c || !c->have_u) return SWR_EINVAL;
   const VsOps* vs = c->vs_cur;
@@ -1008,7 +1046,8 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
                         c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage,
                         c->slice_state.p, (const void*)(uintptr_t)c->slices, c->quad_flag.p, c->quad_tiles.p,
-                        c->quad_count.p, c->geo_bar.p};
+                        c->quad_count.p, c->geo_bar.p, c->dslice_state.p, c->dslice_done.p,
+                        (const void*)(uintptr_t)c->dslice_ok, (const void*)(intptr_t)c->dslice_chunks};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
   if (c->graph_mode && c->gexec && sig == c->gsig) {
     if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;

@@ -16,6 +16,7 @@
 #define SWR_RASTER_SORT 512       // tiles with at most this many bin entries are ordered by k_raster
 #define SWR_SLICES_MAX 8          // overwrite shaders: CTAs (ordered bin slices) per tile of more than
                                   // SWR_RASTER_SORT entries, merged by k_merge_slices
+#define SWR_DSLICES 4             // depth-min shaders: CTAs (runs of whole chunks) per listed heavy tile
 #ifndef SWR_PIX_WALK
 #define SWR_PIX_WALK 1            // k_raster's per-pixel primitive walk (shaders without depth cull or overwrite)
 #endif

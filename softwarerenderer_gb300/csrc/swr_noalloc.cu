@@ -280,6 +280,9 @@ extern "C" int swr_draw_triangle_list_noalloc(const struct SwrUniforms* u, int p
   ra.quad_count = nullptr;
   ra.quad_cap = 0;
   ra.quad_all = 0;
+  ra.dslice = 0;  // no heavy-tile runs: they need the runs' State buffer
+  ra.dslice_state = nullptr;
+  ra.dslice_done = nullptr;
   ps->raster(ra, ntiles, kTile, s);
   if (cudaGetLastError() != cudaSuccess) return SWR_ECUDA;  // a launch failed: the status words are stale
   uint32_t h[16];

@@ -42,6 +42,9 @@ struct PsOps {
   int needs_eq;  // shade() reads the triangle equations: triangles only
   int overwrite;    // SwrOverwrite: large tiles may be rasterized in slices (RasterArgs.slices)
   int state_bytes;  // sizeof(PS::State), per pixel and slice of RasterArgs.slice_state
+  int depth_min;    // SwrDepthMin: heavy tiles may be rasterized in runs (RasterArgs.dslice)
+  int slice_chunks; // SwrRasterSlices: by default tiles of more than this many chunks are (0: none)
+  int chunk;        // SwrRasterChunk: primitives per raster chunk
 };
 
 const VsOps* vs_ops(int id);
@@ -55,7 +58,7 @@ const PsOps* ps_ops(int id);
 // these headers in the caller's unit, so the library checks that both sides agree on the
 // layout of every structure that crosses between them.
 #define SWR_PROGRAM_MAGIC 0x50525753u  // "SWRP"
-#define SWR_PROGRAM_ABI 2u             // bumped with any change to VsOps, PsOps or their argument structs
+#define SWR_PROGRAM_ABI 3u             // bumped with any change to VsOps, PsOps or their argument structs
 #define SWR_PROGRAM_VERTEX 1u
 #define SWR_PROGRAM_PIXEL 2u
 

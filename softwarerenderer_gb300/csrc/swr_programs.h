@@ -220,7 +220,7 @@ SWR_HD uint32_t swr_tex_nearest(const SwrUniforms& u, float tu, float tv) {
 
 // Textured, depth-tested (config: textured cube).  PVar = uv.
 struct PsTexNearest {
-  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1 };
+  enum { AVarCount = 0, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, DepthMin = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -244,7 +244,7 @@ struct PsLambert {
   // 128-primitive chunks: on the dense 1080p mesh 2 % faster than 64 (fewer chunk passes in
   // the silhouette tiles that set the raster's length); 64 suits the other workloads
   enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 5,
-         DepthCull = 0, RasterChunk = 128 };
+         DepthCull = 0, RasterChunk = 128, DepthMin = 1, RasterSlices = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -283,7 +283,7 @@ struct PsLambert {
 // Lambert-lit and textured (nearest RGBA8), depth-tested (config: batched meshes).
 struct PsLambertTex {
   enum { AVarCount = 3, PVarCount = 2, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, RasterOccupancy = 6,
-         DepthCull = 0 };
+         DepthCull = 0, DepthMin = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -307,7 +307,7 @@ struct PsLambertTex {
 
 // Perspective-correct vertex colour, depth-tested (config: triangle soup).  PVar = rgb.
 struct PsVColor {
-  enum { AVarCount = 0, PVarCount = 3, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1 };
+  enum { AVarCount = 0, PVarCount = 3, InterpolateZ = 1, InterpolateW = 1, HasDepth = 1, DepthMin = 1 };
   typedef SwrStateRGBA8 State;
   SWR_HD static void load(State& s, int x, int y, const SwrUniforms& u) { swr_load_rgba8<true>(s, x, y, u); }
   SWR_HD static void store(const State& s, int x, int y, const SwrUniforms& u) { swr_store_rgba8(s, x, y, u, true); }
@@ -692,6 +692,51 @@ struct SwrDepthCull<PS, decltype((void)PS::DepthCull)> {
 // split one pixel's fragments into ordered slices and merge their states.
 SWR_HD void swr_overwrite_merge(SwrStateRGBA8& acc, const SwrStateRGBA8& later) {
   if (later.writes) {
+    acc.color = later.color;
+    acc.winner = later.winner;
+  }
+  acc.frags += later.frags;
+  acc.writes += later.writes;
+}
+
+// Depth-tested RGBA8 shaders whose drawPixel is exactly `s.frags++; if (z < s.depth)
+// swr_write(s, z, shade(p, u), prim)` with a shade() that reads nothing but the fragment
+// (DepthMin = 1 in the shader).  In primitive order such a pixel ends with the depth
+// min(d0, z_1 .. z_n) and the colour and winner of the FIRST fragment reaching it (a later
+// equal z fails the strict test), so a pixel's fragments may be cut into ordered runs, each
+// run from the draw's starting State, and the runs' States merged in order: a later run
+// takes over only with a strictly smaller depth.  The merged colour, depth, winner and
+// fragment count equal the sequential ones; `writes` becomes the sum of the runs' depth-test
+// passes, each against the depth its run started from (at least the sequential count).
+template <class PS, class = void>
+struct SwrDepthMin {
+  enum { value = 0 };
+};
+template <class PS>
+struct SwrDepthMin<PS, decltype((void)PS::DepthMin)> {
+  enum { value = PS::DepthMin && PS::HasDepth && PS::InterpolateZ && !SwrOverwrite<PS>::value };
+};
+
+// Heavy-tile slicing default of a depth-min shader (RasterSlices in the shader): tiles of
+// more than RasterSlices raster chunks of bin entries are rasterized in runs; 0: whole tiles.
+// Measured per workload: it pays where a few heavy tiles set the raster's length (a dense
+// mesh's silhouette), and costs where heavy tiles are many (each run starts from the draw's
+// starting depths, so fewer fragments fail early).
+template <class PS, class = void>
+struct SwrRasterSlices {
+  enum { value = 0 };
+};
+template <class PS>
+struct SwrRasterSlices<PS, decltype((void)PS::RasterSlices)> {
+  enum { value = SwrDepthMin<PS>::value ? PS::RasterSlices : 0 };
+};
+
+// Depth-min shaders' State after two consecutive runs that both started from the same
+// State (SwrDepthMin).  A run that wrote holds a depth below the starting one, so the
+// merged State has writes != 0 exactly when some run's write survives.
+SWR_HD void swr_depth_merge(SwrStateRGBA8& acc, const SwrStateRGBA8& later) {
+  if (later.writes && later.depth < acc.depth) {
+    acc.depth = later.depth;
     acc.color = later.color;
     acc.winner = later.winner;
   }

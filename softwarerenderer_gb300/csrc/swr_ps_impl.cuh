@@ -48,7 +48,9 @@ void run_raster(const RasterArgs& a, uint32_t ntiles, int tile, cudaStream_t s) 
   // submissions run the instantiation without the Span-mode passes
   const bool sliced = SwrOverwrite<PS>::value && a.slices > 1;
   uint32_t grid = sliced ? ntiles * (uint32_t)a.slices : ntiles;
-  if (tile == 16 && !SwrOverwrite<PS>::value) {  // quadrant CTAs (RasterArgs)
+  if (SwrDepthMin<PS>::value && a.dslice) {  // the listed tiles' runs, then the other tiles
+    grid = SWR_DSLICES * a.quad_cap + ntiles;
+  } else if (tile == 16 && !SwrOverwrite<PS>::value) {  // quadrant CTAs (RasterArgs)
     if (a.quad_all) grid = 4 * ntiles;
     else if (a.quad_flag) grid = 4 * a.quad_cap + ntiles;
   }
@@ -99,6 +101,9 @@ PsOps make_ps() {
   o.needs_eq = SwrNeedsEquations<PS>::value;
   o.overwrite = SwrOverwrite<PS>::value;
   o.state_bytes = (int)sizeof(typename PS::State);
+  o.depth_min = SwrDepthMin<PS>::value;
+  o.slice_chunks = SwrRasterSlices<PS>::value;
+  o.chunk = SwrRasterChunk<PS>::value;
   return o;
 }
 

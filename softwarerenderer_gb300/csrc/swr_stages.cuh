@@ -1180,6 +1180,15 @@ struct RasterArgs {
   const uint32_t* quad_count;        // tiles k_sort_cells listed (may exceed quad_cap)
   uint32_t quad_cap;
   int quad_all;
+  // Sliced heavy tiles (depth-min shaders, SwrDepthMin): with dslice set, each tile of the
+  // same list is rasterized by SWR_DSLICES CTAs instead, each over a run of whole chunks of
+  // its ordered bin and from the draw's starting State; each writes its States to
+  // dslice_state, and the last of the tile's CTAs to finish merges them in bin order
+  // (swr_depth_merge) and stores.  CTAs [0, SWR_DSLICES quad_cap) take the listed tiles'
+  // slices; CTA SWR_DSLICES quad_cap + t takes tile t unless it is listed.
+  int dslice;
+  void* dslice_state;      // [slot][slice][TILE * TILE] PS::State
+  uint32_t* dslice_done;   // per slot: the slices finished (zero between draws)
 };
 
 // v <- fl(v + a) repeated k times for 0 <= k <= 7 (steps inside one 8x8 block), as
@@ -1308,6 +1317,17 @@ __device__ __forceinline__ bool z_not_below(float a, float b, float c, float x0,
   return __fsub_rd(zlo, margin) >= dmax;
 }
 
+// A State written by another CTA of the same launch (after its fence): loaded through L2,
+// never from a possibly stale L1 line.
+template <class State>
+__device__ __forceinline__ void swr_ld_state(State& d, const State* p) {
+  static_assert(sizeof(State) % 4 == 0, "States are whole words");
+  uint32_t* o = (uint32_t*)&d;
+  const uint32_t* i = (const uint32_t*)p;
+#pragma unroll
+  for (int k = 0; k < (int)(sizeof(State) / 4); ++k) o[k] = __ldcg(i + k);
+}
+
 template <class PS>
 __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float fx, float fy, int ka, int kb) {
   typedef Rec<PS> RL;
@@ -1394,8 +1414,25 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     slice = blockIdx.x - tile * (uint32_t)g.slices;
   }
   int quad = -1;  // the 8 x 8 quadrant (block) this CTA rasterizes alone, -1: the whole tile
+  int dslot = -1;  // sliced heavy tile: its list slot (slice = its run)
+  if constexpr (SwrDepthMin<PS>::value) {
+    if (g.dslice) {
+      const uint32_t nq = SWR_DSLICES * g.quad_cap;
+      if (blockIdx.x < nq) {
+        const uint32_t slot = blockIdx.x / SWR_DSLICES;
+        if (slot >= min(*g.quad_count, g.quad_cap)) return;
+        tile = g.quad_tiles[slot];
+        slice = blockIdx.x - slot * SWR_DSLICES;
+        dslot = (int)slot;
+      } else {
+        tile = blockIdx.x - nq;
+        if (tile < g.ntiles && g.quad_flag[tile]) return;  // rasterized in slices
+      }
+    }
+  }
   if constexpr (TILE == 16 && !SwrOverwrite<PS>::value) {
-    if (g.quad_all) {
+    if (g.dslice) {
+    } else if (g.quad_all) {
       tile = blockIdx.x >> 2;
       quad = (int)(blockIdx.x & 3u);
     } else if (g.quad_flag) {
@@ -1429,6 +1466,16 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     }
   }
   if (b == e && !sliced) return;  // uniform per CTA
+  // the chunks this CTA rasterizes: the whole bin, or a sliced heavy tile's run
+  uint32_t cb = b, ce = e;
+  int nsl = 1;
+  if (dslot >= 0) {
+    const uint32_t nch = (e - b + CH - 1) / CH;
+    nsl = (int)min(nch, (uint32_t)SWR_DSLICES);
+    if ((int)slice >= nsl) return;  // (uniform per tile: these CTAs take no part)
+    cb = b + (uint32_t)((uint64_t)nch * slice / (uint32_t)nsl) * CH;
+    ce = min(e, b + (uint32_t)((uint64_t)nch * (slice + 1) / (uint32_t)nsl) * CH);
+  }
   const int ti = g.ntargets > 1 ? swr_find_le(g.target_tile_base, g.ntargets, tile) : 0;
   const SwrTargetDesc& T = g.targets[ti];
   const SwrUniforms& U = g.draws[T.first_draw].u;
@@ -1472,8 +1519,8 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
       ssorted[pos < ntot ? pos : 0] = v;
     }
   }
-  for (uint32_t c0 = b; c0 < e; c0 += CH) {
-    const int n = (int)min((uint32_t)CH, e - c0);
+  for (uint32_t c0 = cb; c0 < ce; c0 += CH) {
+    const int n = (int)min((uint32_t)CH, ce - c0);
     __syncthreads();  // the previous chunk's shared state is no longer read; ssorted is complete
     if (threadIdx.x < n) sids[threadIdx.x] = self_sort ? ssorted[c0 - b + threadIdx.x] : g.bin[c0 + threadIdx.x];
     if (threadIdx.x == 0) snpart = 0;
@@ -1493,7 +1540,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     bool cull_tile = false;
     bool my_ok = false;
     if constexpr (kCull) {
-      cull_tile = e - b > (uint32_t)CH;
+      cull_tile = ce - cb > (uint32_t)CH;
       if (cull_tile) {
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
@@ -1970,6 +2017,48 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
         PS::drawPixel(pd, prim_id(g, r, sids[k]), st[q], g.draws[__float_as_int(r[1])].u);
       }
+    }
+  }
+  if constexpr (SwrDepthMin<PS>::value) {
+    if (dslot >= 0) {
+      // this run's States, then the last run to finish merges the tile's runs in bin order
+      // (each thread owns the same pixels in every run's CTA)
+      typename PS::State* ss = (typename PS::State*)g.dslice_state + (size_t)dslot * SWR_DSLICES * (TILE * TILE);
+#pragma unroll
+      for (int q = 0; q < PPT; ++q)
+        if (in[q]) {
+          ss[(size_t)slice * (TILE * TILE) + (py[q] - oy) * TILE + (px[q] - ox)] = st[q];
+          passes += st[q].writes;
+        }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) snc = atomicAdd(&g.dslice_done[dslot], 1u) == (uint32_t)(nsl - 1);
+      __syncthreads();
+      if (snc) {
+        __threadfence();
+#pragma unroll
+        for (int q = 0; q < PPT; ++q)
+          if (in[q]) {
+            const int pi = (py[q] - oy) * TILE + (px[q] - ox);
+            typename PS::State m;
+            swr_ld_state(m, ss + pi);
+            for (int sl = 1; sl < nsl; ++sl) {
+              typename PS::State o;
+              swr_ld_state(o, ss + (size_t)sl * (TILE * TILE) + pi);
+              swr_depth_merge(m, o);
+            }
+            PS::store(m, px[q], py[q], U);
+          }
+        if (threadIdx.x == 0) g.dslice_done[dslot] = 0u;  // ready for the next draw
+      }
+      uint32_t tot, ptot;
+      swr_block_exscan(frags, sfr, &tot);
+      swr_block_exscan(passes, sfr, &ptot);
+      if (threadIdx.x == 0 && tot) {
+        atomicAdd((unsigned long long*)&g.status_w[SWR_ST_SHADED_LO], (unsigned long long)tot);
+        atomicAdd((unsigned long long*)&g.status_w[SWR_ST_PASSES_LO], (unsigned long long)ptot);
+      }
+      return;
     }
   }
 #pragma unroll

@@ -103,6 +103,13 @@ class Context:
         self.L.swr_set_tile_split.restype = ctypes.c_int
         _lib.check(self.L.swr_set_tile_split(self.h, int(bool(on))), "set_tile_split")
 
+    def set_tile_slicing(self, chunks=-1):
+        """Tiles of more than `chunks` raster chunks rasterized in four runs (depth-min
+        shaders); 0: every tile whole by one CTA; -1: the shader's own setting."""
+        self.L.swr_set_tile_slicing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.swr_set_tile_slicing.restype = ctypes.c_int
+        _lib.check(self.L.swr_set_tile_slicing(self.h, int(chunks)), "set_tile_slicing")
+
     def set_profiling(self, on=True):
         _lib.check(self.L.swr_set_profiling(self.h, int(bool(on))), "set_profiling")
 

@@ -540,6 +540,36 @@ def random_scene(seed: int, direct: Optional[bool] = None, draw_mode: Optional[D
                  texture=tex, checker=int(rng.integers(2, 20)))
 
 
+def stack_scene(seed: int, n: int, ps: PS = PS.VCOLOR, raster: RasterMode = RasterMode.Block,
+                width: int = 48, height: int = 40) -> Scene:
+    """A pile of n triangles over a small target: each triangle 3-30 px across, at one of six
+    constant depths (so equal depths tie often), either winding, no culling.  Its tiles hold
+    hundreds to thousands of bin entries: the heavy-tile path of the tile rasterizer."""
+    rng = np.random.default_rng(50_000 + seed)
+    c = rng.random((n, 1, 2)) * np.array([width, height])
+    size = 3.0 + 27.0 * rng.random((n, 1, 1))
+    pts = c + (rng.random((n, 3, 2)) - 0.5) * size
+    ndc = np.empty((n, 3, 3), np.float64)
+    ndc[:, :, 0] = pts[:, :, 0] / (width * 0.5) - 1.0
+    ndc[:, :, 1] = 1.0 - pts[:, :, 1] / (height * 0.5)
+    ndc[:, :, 2] = np.array([-0.5, -0.25, 0.0, 0.25, 0.5, 0.75])[rng.integers(0, 6, n)][:, None]
+    pos = ndc.reshape(-1, 3)
+    nv = 3 * n
+    if ps in (PS.LAMBERT, PS.LAMBERT_TEX):
+        vs = VS.POS_NRM_UV
+        nrm = rng.random((nv, 3)) * 2 - 1
+        attribs = [(np.concatenate([pos, nrm], 1).astype(np.float32), 24),
+                   (rng.random((nv, 2)).astype(np.float32), 8)]
+    else:
+        vs = VS.POS_RGB
+        attribs = [(np.concatenate([pos, rng.random((nv, 3))], 1).astype(np.float32), 24)]
+    tex = small_texture(rng, False) if ps in (PS.TEX_NEAREST, PS.LAMBERT_TEX) else None
+    return Scene(name=f"stack{n}s{seed}", vs=vs, ps=ps, width=width, height=height, cull=CullMode.None_,
+                 raster=raster, viewport=(0, 0, width, height), scissor=(0, 0, width, height),
+                 attribs=attribs, indices=np.arange(nv, dtype=np.int32), light=np.array([0.3, -0.2, 0.93, 0.15], np.float32),
+                 texture=tex, checker=5)
+
+
 # ----------------------------------------------------------------------------
 # Benchmark.cpp-shaped scene and spec-driven construction (fixtures, tests, bench)
 

@@ -10,10 +10,16 @@ def oracle_render(port, scene, threads=0):
     return t.arrays(), st
 
 
-def gpu_render(scene, tile=16, split=False):
-    """tile: 8, 16 or 32 (swr_set_tile_size); split: heavy 16-px tiles as quadrant CTAs."""
+def gpu_render(scene, tile=16, split=False, slicing=-1):
+    """tile: 8, 16 or 32 (swr_set_tile_size); split: heavy 16-px tiles as quadrant CTAs (in
+    place of the depth-min shaders' heavy-tile runs); slicing: swr_set_tile_slicing's chunk
+    threshold for those runs (-1: the shader's default, 0: whole tiles)."""
     from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
     ds = DeviceScene(scene, tile=tile)
+    if split:
+        slicing = 0
+    if slicing != -1:
+        ds.rast.ctx.set_tile_slicing(slicing)
     if split:
         ds.rast.ctx.set_tile_split(True)
     tg = DeviceTarget(scene)
