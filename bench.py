@@ -42,12 +42,13 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
 # Means over the headline k_raster launches of the 32 timed poses, from ncu captures of
 # `python bench.py --steps 32 --warmup 3 --no-...` (profiles/k_raster_lambert_sphere7_1080p.md):
 # dram__bytes_read.sum + dram__bytes_write.sum with the L2 as the frame's earlier kernels
-# leave it (--cache-control none: the setup records and the cleared target are still in L2)
-# and with the L2 flushed before every launch (ncu's default), and smsp__inst_executed.sum
-# (warp instructions) per launch.
-NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 4531120}
-NCU_DRAM_BYTES_COLD = {"raster": 19736520}
-NCU_WARP_INST_PER_LAUNCH = {"raster": 38414947}
+# leave it (--cache-control none: the setup records and the cleared target are still in L2;
+# the writes are dirty lines of the L2 flush buffer that the launch's own stores evict) and
+# with the L2 flushed before every launch (ncu's default), and smsp__inst_executed.sum (warp
+# instructions) per launch.
+NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 7399584}
+NCU_DRAM_BYTES_COLD = {"raster": 19747448}
+NCU_WARP_INST_PER_LAUNCH = {"raster": 42318430}
 SMS = 152
 
 

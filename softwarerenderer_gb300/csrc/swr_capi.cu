@@ -19,6 +19,7 @@ namespace swr {
 // colour writes.
 constexpr int kStatusWords = 16;
 constexpr int kSingleSlots = 8;            // pinned descriptor slots of single draws
+constexpr int kBatchSlots = 2;             // pinned descriptor slots (and cached graphs) of batches
 constexpr size_t kSingleSlotBytes = 1024;  // >= sizeof(SwrDrawDesc) + sizeof(SwrTargetDesc)
 constexpr size_t kBigSortSmem = 128 * 1024;  // shared memory of a k_sort_big CTA (bounds one warp's bitmap)
 constexpr int kBigSortWarps = 1216;          // warps of k_sort_big (8 per SM)
@@ -45,16 +46,26 @@ uint32_t slice_cap(uint32_t ntiles) {
 // Descriptor upload from pinned host staging (device-accessible under unified addressing)
 // by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
 // large host<->device copy the application runs on another stream, delaying the draw.
+// The same kernel zeroes the draw's small per-draw words (counters, single-draw bases), which
+// as separate memsets would each be one more operation (graph node) ahead of the draw.
 struct StageCopy {
   void* dst[6];
   const void* src[6];
   uint32_t words[6];
-  int n;
+  int n = 0;
+  uint32_t* zero[6];
+  uint32_t zero_words[6];
+  int nz = 0;
   void add(void* d, const void* s, size_t bytes) {
     dst[n] = d;
     src[n] = s;
     words[n] = (uint32_t)(bytes / 4);
     ++n;
+  }
+  void clear(void* d, size_t bytes) {
+    zero[nz] = (uint32_t*)d;
+    zero_words[nz] = (uint32_t)(bytes / 4);
+    ++nz;
   }
 };
 constexpr int kStageCopyBlocks = 8;
@@ -62,6 +73,9 @@ static_assert(sizeof(SwrDrawDesc) % 4 == 0 && sizeof(SwrTargetDesc) % 4 == 0, "d
 
 __global__ void k_stage_copy(const StageCopy sc) {
   swr_pdl_entry();
+  if (blockIdx.x == 0)
+    for (int k = 0; k < sc.nz; ++k)
+      for (uint32_t i = threadIdx.x; i < sc.zero_words[k]; i += blockDim.x) sc.zero[k][i] = 0u;
   for (int k = 0; k < sc.n; ++k) {
     const uint32_t* s = (const uint32_t*)sc.src[k];
     uint32_t* d = (uint32_t*)sc.dst[k];
@@ -176,14 +190,18 @@ struct swr_context {
   cudaEvent_t single_ev[swr::kSingleSlots] = {};
   bool single_pending[swr::kSingleSlots] = {};
   int single_next = 0;
-  cudaEvent_t stage_read = nullptr;  // recorded after the staging copies of the last batch
-  bool stage_pending = false;
+  int single_cur = -1;               // the slot of the single draw being queued
+  // batch descriptors: kBatchSlots pinned staging slots used in turn, each with the event
+  // recorded after the last draw that read it and the CUDA graph captured over it
+  int stage_next = 0;
+  cudaEvent_t stage_ev[swr::kBatchSlots] = {};
+  bool stage_pending[swr::kBatchSlots] = {};
   bool graph_mode = false;
   bool capturing = false;
-  cudaGraphExec_t gexec = nullptr;
+  cudaGraphExec_t gexec[swr::kBatchSlots] = {};
   cudaStream_t cap_stream = nullptr;  // graphs are recorded here, then launched on the caller's stream
-  uint64_t gsig = 0;
-  uint64_t glaunches = 0;  // kernels per replay of the cached graph
+  uint64_t gsig[swr::kBatchSlots] = {};
+  uint64_t glaunches[swr::kBatchSlots] = {};  // kernels per replay of each cached graph
 
   void attach_budget() {
     swr::Buffer* all[] = {&draws, &targets, &draw_vbase, &draw_bbase, &target_tile_base, &ptv, &clipv,
@@ -402,7 +420,7 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   const bool quad_list = quads && c->quad_mode == 1;
   const bool listed = dsl || quad_list;
   const uint32_t qcap = dsl ? slice_cap(ntiles) : quad_cap(ntiles);
-  if (listed) cudaMemsetAsync(c->quad_count.p, 0, 4, s);
+  // (quad_count was zeroed by the draw's k_stage_copy)
   swr::launch(k_sort_cells, (ntiles + warps_per_block - 1) / warps_per_block, 256, 0, s, st, cstart, ntiles, c->cap_pairs, c->keys0.as<uint32_t>(), c->vals0.as<uint32_t>(), use_big ? big + 2 : nullptr,
       big, (uint32_t)SWR_RASTER_SORT,
       listed ? c->quad_flag.as<uint8_t>() : nullptr, c->quad_tiles.as<uint32_t>(), c->quad_count.as<uint32_t>(), qcap,
@@ -519,7 +537,9 @@ int lp_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, int v
 
 // Descriptors of a single draw are staged in a ring of pinned slots (a copy from pageable
 // memory may block the host until the stream drains); a slot is rewritten only after the
-// copy that read it has run, so the host can queue kSingleSlots draws ahead of the GPU.
+// draw that read it has run, so the host can queue kSingleSlots draws ahead of the GPU.
+// The slot's event is recorded after the draw's last kernel (end_single): an event between
+// two kernels of the draw would hold back the second one's programmatic early launch.
 static_assert(sizeof(SwrDrawDesc) + sizeof(SwrTargetDesc) <= kSingleSlotBytes, "descriptor slot size");
 
 int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, cudaStream_t s) {
@@ -536,19 +556,37 @@ int upload_single(swr_context* c, const SwrDrawDesc& D, const SwrTargetDesc& T, 
   memcpy(h, &D, sizeof(D));
   memcpy(h + sizeof(D), &T, sizeof(T));
   StageCopy sc;
-  sc.n = 0;
   sc.add(c->draws.p, h, sizeof(D));
   sc.add(c->targets.p, h + sizeof(D), sizeof(T));
+  // a single draw's vertex, batch and tile bases are 0; the per-draw working counters and
+  // the heavy-tile list restart (flags and fragment totals are sticky)
+  sc.clear(c->draw_vbase.p, 4);
+  sc.clear(c->draw_bbase.p, 4);
+  sc.clear(c->target_tile_base.p, 4);
+  sc.clear(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 5 * 4);
+  sc.clear(c->quad_count.p, 4);
   swr::launch(k_stage_copy, 1, 256, 0, s, sc);
   c->launches += 1;
-  cudaEventRecord(c->single_ev[slot], s);
-  c->single_pending[slot] = true;
-  cudaMemsetAsync(c->draw_vbase.p, 0, 4, s);
-  cudaMemsetAsync(c->draw_bbase.p, 0, 4, s);
-  cudaMemsetAsync(c->target_tile_base.p, 0, 4, s);
-  // reset the per-draw working counters (flags and fragment totals are sticky)
-  cudaMemsetAsync(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 0, 5 * 4, s);
+  c->single_cur = slot;
   return cuda_err(cudaGetLastError());
+}
+
+// A batch's staging slot is free again once the draw (or graph replay) that read it has run:
+// its event is recorded after the whole draw, outside any captured graph (an event node
+// inside the graph would hold back the programmatic early launch of the kernel after it).
+int end_batch(swr_context* c, int slot, cudaStream_t s, int rc) {
+  cudaEventRecord(c->stage_ev[slot], s);
+  c->stage_pending[slot] = true;
+  return rc;
+}
+
+int end_single(swr_context* c, cudaStream_t s, int rc) {
+  if (c->single_cur >= 0) {
+    cudaEventRecord(c->single_ev[c->single_cur], s);
+    c->single_pending[c->single_cur] = true;
+    c->single_cur = -1;
+  }
+  return rc;
 }
 
 SwrTargetDesc make_target(const swr_context* c) {
@@ -592,9 +630,11 @@ int swr_destroy(swr_context* c) {
   if (!c) return SWR_EINVAL;
   if (c->status_host) cudaFreeHost(c->status_host);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (int i = 0; i < kBatchSlots; ++i) {
+    if (c->gexec[i]) cudaGraphExecDestroy(c->gexec[i]);
+    if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+  }
   if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
-  if (c->stage_read) cudaEventDestroy(c->stage_read);
   if (c->single_stage) cudaFreeHost(c->single_stage);
   for (int i = 0; i < kSingleSlots; ++i)
     if (c->single_ev[i]) cudaEventDestroy(c->single_ev[i]);
@@ -856,8 +896,9 @@ int swr_draw_elements(swr_context* c, int mode, uint64_t count, const uint32_t* 
   }
   mark(c, 2, s);
   c->last_ntiles = ntiles;
-  if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, T, s);
-  return raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s, 1, c->raster_mode != SWR_RASTER_BLOCK);
+  if (mode != SWR_DRAW_TRIANGLE) return end_single(c, s, lp_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, T, s));
+  return end_single(c, s, raster_stage(c, ps, vs->S, 8, 8 + vs->A, vs->A, vs->P, ntiles, s, 1,
+                                       c->raster_mode != SWR_RASTER_BLOCK));
 }
 
 int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nverts, const int32_t* indices,
@@ -899,8 +940,9 @@ int swr_draw_list(swr_context* c, int mode, const float* vertices, uint64_t nver
   }
   mark(c, 2, s);
   c->last_ntiles = ntiles;
-  if (mode != SWR_DRAW_TRIANGLE) return lp_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, T, s);
-  return raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s, 1, c->raster_mode != SWR_RASTER_BLOCK);
+  if (mode != SWR_DRAW_TRIANGLE) return end_single(c, s, lp_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, T, s));
+  return end_single(c, s, raster_stage(c, ps, ps->S, 8, 8 + ps->A, ps->A, ps->P, ntiles, s, 1,
+                                       c->raster_mode != SWR_RASTER_BLOCK));
 }
 
 int swr_set_graph_mode(swr_context* c, int on) {
@@ -1014,21 +1056,31 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
             c->draw_vbase.ensure(4 * n + 16) && c->draw_bbase.ensure(4 * n + 16) && c->draw_pbase.ensure(4 * n + 16) &&
             c->target_tile_base.ensure(4 * ntg + 16);
   if (!ok) return SWR_ENOMEM;
-  // pinned staging; wait until the previous batch's copies have read it
+  // pinned staging, kBatchSlots slots used in turn; wait until the last draw that read this
+  // slot has run (the draw kBatchSlots calls back, normally long finished)
   const size_t bytes = sizeof(SwrDrawDesc) * n + sizeof(SwrTargetDesc) * ntg + 4 * (2 * n + ntg) + 64;
-  if (c->stage_pending && c->stage_read) {
-    if ((rc = cuda_err(cudaEventSynchronize(c->stage_read)))) return rc;
-    c->stage_pending = false;
+  const int slot = c->stage_next;
+  c->stage_next = (slot + 1) % kBatchSlots;
+  if (c->stage_pending[slot]) {
+    if ((rc = cuda_err(cudaEventSynchronize(c->stage_ev[slot])))) return rc;
+    c->stage_pending[slot] = false;
   }
-  if (bytes > c->stage_bytes) {
+  if (bytes > c->stage_bytes / kBatchSlots) {
+    for (int k = 0; k < kBatchSlots; ++k)  // the other slots' draws may still read them
+      if (c->stage_pending[k]) {
+        if ((rc = cuda_err(cudaEventSynchronize(c->stage_ev[k])))) return rc;
+        c->stage_pending[k] = false;
+      }
     if (c->stage) cudaFreeHost(c->stage);
     c->stage = nullptr;
     c->stage_bytes = 0;
-    if ((rc = cuda_err(cudaMallocHost((void**)&c->stage, bytes * 2)))) return rc;
-    c->stage_bytes = bytes * 2;
+    if ((rc = cuda_err(cudaMallocHost((void**)&c->stage, bytes * 2 * kBatchSlots)))) return rc;
+    c->stage_bytes = bytes * 2 * kBatchSlots;
   }
-  if (!c->stage_read && (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_read, cudaEventDisableTiming)))) return rc;
-  unsigned char* h = c->stage;
+  for (int k = 0; k < kBatchSlots; ++k)
+    if (!c->stage_ev[k] && (rc = cuda_err(cudaEventCreateWithFlags(&c->stage_ev[k], cudaEventDisableTiming))))
+      return rc;
+  unsigned char* h = c->stage + (size_t)slot * (c->stage_bytes / kBatchSlots);
   const size_t o_d = 0, o_t = o_d + sizeof(SwrDrawDesc) * n, o_vb = o_t + sizeof(SwrTargetDesc) * ntg;
   const size_t o_bb = o_vb + 4 * n, o_tb = o_bb + 4 * n;
   memcpy(h + o_d, D.data(), sizeof(SwrDrawDesc) * n);
@@ -1044,16 +1096,15 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   const void* bufs[] = {c->ptv.p, c->clipv.p, c->clip_table.p, c->clip_slot.p, c->tri_flags.p, c->batch_counts.p,
                         c->tris.p, c->recs.p, c->tile_count.p, c->keys0.p, c->vals0.p, c->cell_count.p,
                         c->cell_start.p, c->scratch.p, c->draws.p, c->targets.p, c->draw_vbase.p,
-                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, c->stage,
+                        c->draw_bbase.p, c->target_tile_base.p, c->draw_pbase.p, c->big_cells.p, h,
                         c->slice_state.p, (const void*)(uintptr_t)c->slices, c->quad_flag.p, c->quad_tiles.p,
                         c->quad_count.p, c->geo_bar.p, c->dslice_state.p, c->dslice_done.p,
                         (const void*)(uintptr_t)c->dslice_ok, (const void*)(intptr_t)c->dslice_chunks};
   for (const void* b : bufs) mix((uint64_t)(uintptr_t)b);
-  if (c->graph_mode && c->gexec && sig == c->gsig) {
-    if ((rc = cuda_err(cudaGraphLaunch(c->gexec, s)))) return rc;
-    c->stage_pending = true;
-    c->launches += c->glaunches;
-    return SWR_OK;
+  if (c->graph_mode && c->gexec[slot] && sig == c->gsig[slot]) {
+    if ((rc = cuda_err(cudaGraphLaunch(c->gexec[slot], s)))) return rc;
+    c->launches += c->glaunches[slot];
+    return end_batch(c, slot, s, SWR_OK);
   }
   cudaGraph_t graph = nullptr;
   const uint64_t launches0 = c->launches;
@@ -1069,21 +1120,19 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
   int q = SWR_OK;
   {
     StageCopy sc;
-    sc.n = 0;
     sc.add(c->draws.p, h + o_d, sizeof(SwrDrawDesc) * n);
     sc.add(c->targets.p, h + o_t, sizeof(SwrTargetDesc) * ntg);
     sc.add(c->draw_vbase.p, h + o_vb, 4 * n);
     sc.add(c->draw_bbase.p, h + o_bb, 4 * n);
     sc.add(c->target_tile_base.p, h + o_tb, 4 * ntg);
+    // the per-draw working counters and the heavy-tile list restart (flags and fragment
+    // totals are sticky)
+    sc.clear(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 5 * 4);
+    sc.clear(c->quad_count.p, 4);
     swr::launch(k_stage_copy, kStageCopyBlocks, 256, 0, s, sc);
     c->launches += 1;
     q = cuda_err(cudaGetLastError());
   }
-  // the host waits on this event before it rewrites the staging area; inside a capture
-  // only an external record becomes a node the host can wait on
-  q = q ? q : cuda_err(c->capturing ? cudaEventRecordWithFlags(c->stage_read, s, cudaEventRecordExternal)
-                                    : cudaEventRecord(c->stage_read, s));
-  q = q ? q : cuda_err(cudaMemsetAsync(c->status.as<uint32_t>() + SWR_ST_CLIP_SLOTS, 0, 5 * 4, s));
   q = q ? q : cuda_err(cudaGetLastError());
   uint32_t* st = c->status.as<uint32_t>();
   mark(c, 0, s);
@@ -1129,17 +1178,16 @@ int swr_draw_batch(swr_context* c, const swr_draw_item* items, int n, void* stre
       if (graph) cudaGraphDestroy(graph);
       return rc ? rc : rc2;
     }
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
-    rc = cuda_err(cudaGraphInstantiate(&c->gexec, graph, 0));
+    if (c->gexec[slot]) cudaGraphExecDestroy(c->gexec[slot]);
+    c->gexec[slot] = nullptr;
+    rc = cuda_err(cudaGraphInstantiate(&c->gexec[slot], graph, 0));
     cudaGraphDestroy(graph);
     if (rc) return rc;
-    c->gsig = sig;
-    c->glaunches = c->launches - launches0;
-    if ((rc = cuda_err(cudaGraphLaunch(c->gexec, launch_stream)))) return rc;
+    c->gsig[slot] = sig;
+    c->glaunches[slot] = c->launches - launches0;
+    if ((rc = cuda_err(cudaGraphLaunch(c->gexec[slot], launch_stream)))) return rc;
   }
-  c->stage_pending = true;
-  return rc;
+  return end_batch(c, slot, launch_stream, rc);
 }
 
 int swr_finish(swr_context* c, void* stream, swr_stats* stats) {
