@@ -1399,6 +1399,11 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   // small primitives with large ones, the per-lane loops cost 30 % more raster time.)
   constexpr bool kPixWalk = SWR_PIX_WALK && kCompact && !kCull && !SwrOverwrite<PS>::value;
   __shared__ uint64_t spm[kPixWalk ? TILE * TILE * HW : 1];
+  // per (primitive, block): the primitive's covered pixels in the tile's earlier blocks, so a
+  // compacted fragment's slot is sex + spre + its rank in the block's mask (a compacted
+  // primitive covers at most SMALL = 64 pixels of the tile: its prefixes fit a byte)
+  __shared__ uint8_t spre[kCompact ? CH * NB : 1];
+  __shared__ int32_t spid[CH];  // the primitives' ids as drawPixel sees them
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t frags = 0, passes = 0;
@@ -1731,9 +1736,11 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         culled = false;
         if (k >= n) return;
         const float* r = srec + k * RL::R;
+        spid[k] = prim_id(g, r, sids[k]);
         if (!(__float_as_int(r[0]) & 1)) return;
         for (int j = 0; j < NB; ++j) {
           const uint64_t m = smask[k * NB + j];
+          if (kCompact) spre[k * NB + j] = (uint8_t)min(cnt, 255u);
           cnt += __popc((uint32_t)m) + __popc((uint32_t)(m >> 32));
         }
         if (kCull && try_cull && cnt) {
@@ -1878,10 +1885,8 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             const float* r = srec + k * RL::R;
             frags++;
             if (scomp[k]) {
-              int rank = __popcll(m & ((1ull << bit) - 1ull));
-              for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
-              const int f = (int)sex[k] + rank;
-              PS::apply(st[q], sfz[f], sfc[f], prim_id(g, r, sids[k]));
+              const int f = (int)sex[k] + (int)spre[k * NB + blk[q]] + __popcll(m & ((1ull << bit) - 1ull));
+              PS::apply(st[q], sfz[f], sfc[f], spid[k]);
               continue;
             }
             const bool blockmode = !SPAN || (__float_as_int(r[0]) & 2);
@@ -1907,7 +1912,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
             if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
             build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
-            PS::drawPixel(pd, prim_id(g, r, sids[k]), st[q], g.draws[__float_as_int(r[1])].u);
+            PS::drawPixel(pd, spid[k], st[q], g.draws[__float_as_int(r[1])].u);
           }
         }
         continue;
@@ -1986,10 +1991,8 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         const float* r = srec + k * RL::R;
         frags++;
         if (scomp[k]) {
-          int rank = __popcll(m & ((1ull << bit) - 1ull));
-          for (int j = 0; j < blk[q]; ++j) rank += __popcll(mk[j]);
-          const int f = (int)sex[k] + rank;
-          PS::apply(st[q], sfz[f], sfc[f], prim_id(g, r, sids[k]));
+          const int f = (int)sex[k] + (int)spre[k * NB + blk[q]] + __popcll(m & ((1ull << bit) - 1ull));
+          PS::apply(st[q], sfz[f], sfc[f], spid[k]);
           continue;
         }
         const bool blockmode = !SPAN || (__float_as_int(r[0]) & 2);
@@ -2015,7 +2018,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         pd.z = build_z<PS>(eq, blockmode, fx, fy, ka, kb);
         if (RL::IZ && PS::earlyReject(pd.z, st[q])) continue;
         build_pixel<PS>(eq, blockmode, fx, fy, ka, kb, pd);
-        PS::drawPixel(pd, prim_id(g, r, sids[k]), st[q], g.draws[__float_as_int(r[1])].u);
+        PS::drawPixel(pd, spid[k], st[q], g.draws[__float_as_int(r[1])].u);
       }
     }
   }
