@@ -361,7 +361,7 @@ bool geometry_front(swr_context* c, const VsOps* vs, const SwrDrawDesc* draws, i
     cudaGetLastError();
     return false;
   }
-  c->launches -= 1;  // one launch for the three counted kernels
+  c->launches -= nverts ? 2 : 1;  // one launch for the (up to) three counted kernels
   return true;
 }
 
