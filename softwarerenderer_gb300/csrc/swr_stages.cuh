@@ -579,7 +579,11 @@ __device__ __forceinline__ Edge make_edge(float x0, float y0, float x1, float y1
   return e;
 }
 
-__device__ __forceinline__ bool edge_test(float v, bool tie) { return v > 0.0f || (v == 0.0f && tie); }
+// EdgeEquation::test (EdgeEquation.h): v > 0, or v == 0 on a tie edge.  Written as one
+// comparison against a per-edge threshold: with denormals kept (no flush to zero) no float
+// lies strictly between 0 and 2^-149, so v > 0 is v >= 2^-149; v == 0 (either zero) with
+// the tie is v >= 0; NaN fails both, as it fails the reference's two comparisons.
+__device__ __forceinline__ bool edge_test(float v, bool tie) { return v >= (tie ? 0.0f : 0x1p-149f); }
 
 __device__ __forceinline__ void param_eq(float p0, float p1, float p2, const Edge& e0, const Edge& e1,
                                          const Edge& e2, float f, float* o) {
