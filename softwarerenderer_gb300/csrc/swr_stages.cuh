@@ -1381,6 +1381,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
   __shared__ Color sfc[FB];
   __shared__ uint32_t sfr[32];
   __shared__ uint32_t snc;
+  __shared__ uint32_t suncomp;  // some primitive of the chunk covers pixels and was not compacted
   __shared__ uint16_t spart[CH * NB];  // partially covered (primitive, block) pairs
   __shared__ uint32_t snpart;
   __shared__ uint32_t ssorted[SWR_RASTER_SORT];  // the tile's ordered bin (self-sorted tiles)
@@ -1663,25 +1664,17 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
     } else {
       __syncthreads();
     }
-    // B2: partially covered blocks, one row per lane (8 lanes per block)
+    // B2: partially covered blocks, one row per lane (8 lanes per block); each lane stores
+    // its row's byte of the block's mask (bit row * 8 + col of the little-endian word)
     {
       const int np8 = (int)snpart * SWR_BLOCK;
-      for (int t0 = 0; t0 < np8; t0 += 256) {
-        const int t = t0 + threadIdx.x;
-        uint64_t bits = 0;
-        int i = 0;
-        if (t < np8) {
-          i = spart[t >> 3];
-          const int row = t & 7;
-          const int k = i / NB, j = i - k * NB;
-          const float* r = srec + k * RL::R;
-          bits = (uint64_t)block_row_bits(r, __float_as_int(r[0]), ox + (j % NBX) * SWR_BLOCK,
-                                          oy + (j / NBX) * SWR_BLOCK, row) << (row * 8);
-        }
-        bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
-        bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
-        bits |= __shfl_xor_sync(0xffffffffu, bits, 4);
-        if (t < np8 && (t & 7) == 0) smask[i] = bits;
+      for (int t = threadIdx.x; t < np8; t += 256) {
+        const int i = spart[t >> 3];
+        const int row = t & 7;
+        const int k = i / NB, j = i - k * NB;
+        const float* r = srec + k * RL::R;
+        ((uint8_t*)&smask[i])[row] = (uint8_t)block_row_bits(r, __float_as_int(r[0]), ox + (j % NBX) * SWR_BLOCK,
+                                                             oy + (j / NBX) * SWR_BLOCK, row);
       }
     }
     __syncthreads();
@@ -1791,6 +1784,7 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
           }
         }
         uint32_t carry = 0, hi = 0;
+        bool unc = false;
 #pragma unroll
         for (int w = 0; w < NW; ++w) {
           const uint32_t ex = carry + inc[w] - cand[w];
@@ -1801,9 +1795,14 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
             scomp[w * 32 + lane] = comp ? 1 : 0;
           }
           if (comp && cnt[w]) hi = max(hi, ex + cnt[w]);
+          unc |= !comp && cnt[w] != 0u;
         }
         const uint32_t nc_max = __reduce_max_sync(0xffffffffu, hi);
-        if (lane == 0) snc = nc_max;
+        const bool any_unc = __any_sync(0xffffffffu, unc);
+        if (lane == 0) {
+          snc = nc_max;
+          suncomp = any_unc ? 1u : 0u;
+        }
       }
     }
     __syncthreads();
@@ -1868,11 +1867,13 @@ __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRa
         uint64_t todo[HW];
 #pragma unroll
         for (int w = 0; w < HW; ++w) todo[w] = 0;
+        if (suncomp) {  // (uniform; a chunk of compacted primitives only has nothing to ballot)
 #pragma unroll
-        for (int w = 0; w < NW; ++w) {
-          const int k = w * 32 + lane;
-          const bool h = k < n && !scomp[k] && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
-          todo[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
+          for (int w = 0; w < NW; ++w) {
+            const int k = w * 32 + lane;
+            const bool h = k < n && !scomp[k] && ((uint32_t)(smask[k * NB + blk[q]] >> (half * 32)) != 0u);
+            todo[w >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, h) << ((w & 1) * 32);
+          }
         }
         const int bit = (py[q] & 7) * 8 + (px[q] & 7);
         if (!in[q]) continue;
