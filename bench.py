@@ -46,9 +46,9 @@ WORKLOAD = ("icosphere subdivision 7 (163,842 v / 327,680 t, pos+normal 24 B + u
 # the writes are dirty lines of the L2 flush buffer that the launch's own stores evict) and
 # with the L2 flushed before every launch (ncu's default), and smsp__inst_executed.sum (warp
 # instructions) per launch.
-NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 7399584}
-NCU_DRAM_BYTES_COLD = {"raster": 19747448}
-NCU_WARP_INST_PER_LAUNCH = {"raster": 42318430}
+NCU_DRAM_BYTES_PER_LAUNCH = {"raster": 7464800}
+NCU_DRAM_BYTES_COLD = {"raster": 19747224}
+NCU_WARP_INST_PER_LAUNCH = {"raster": 35816046}
 SMS = 152
 
 
