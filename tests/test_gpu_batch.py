@@ -52,14 +52,17 @@ def test_batch_shared_target_in_item_order(gpu_lib, port):
         assert np.asarray(t.arrays()[k]).tobytes() == np.asarray(got[k]).tobytes(), k
 
 
-@pytest.mark.parametrize("kind", ["cube", "sphere5"])
+@pytest.mark.parametrize("kind", ["cube", "sphere5", "sphere7"])
 def test_graph_mode_single_draws(gpu_lib, port, kind):
     """Triangle drawElements in graph mode run as one-item batches: the first draw captures
-    the graph, later draws (other poses, the other of two targets) replay it."""
+    the graph, later draws (other poses, the other of two targets) replay it.  The dense
+    1080p mesh (the bench's frame) also runs its heavy tiles as runs of chunks, whose
+    completion counters must return to zero between replays."""
     from softwarerenderer_gb300.device import DeviceScene, DeviceTarget
     from .parity import diff, oracle_render
-    mk = (lambda k: scenes.cube_scene(k)) if kind == "cube" else (
-        lambda k: scenes.sphere_scene(k, level=5, width=640, height=360))
+    mk = {"cube": lambda k: scenes.cube_scene(k),
+          "sphere5": lambda k: scenes.sphere_scene(k, level=5, width=640, height=360),
+          "sphere7": lambda k: scenes.sphere_scene(k)}[kind]
     sc0 = mk(0)
     ds = DeviceScene(sc0)
     ds.rast.ctx.set_graph_mode(True)
