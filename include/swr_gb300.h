@@ -307,8 +307,10 @@ SWR_API int swr_write_image(const char* path, const void* pixels, int width, int
  * or cudaFree.  Limits: <= 4096 triangles, <= 12288 vertices, a target of <= 16384 tiles
  * of 16 x 16 pixels (e.g. 2048 x 2048); larger inputs return SWR_EINVAL up front, and more
  * than 262144 (tile, triangle) bin entries return SWR_EOVERFLOW with the target untouched.
- * Synchronous: returns after the stream has drained; *fragments (may be NULL) receives
- * the drawPixel count.  The first call on a device is its set-up: it looks up the array's
+ * Synchronous: returns after the stream has drained, so no call can be captured in a CUDA
+ * graph (it copies its descriptors from pageable memory and synchronises the stream);
+ * *fragments (may be NULL) receives the drawPixel count.  Past the first call it allocates
+ * nothing.  The first call on a device is its set-up: it looks up the array's
  * address (cudaGetSymbolAddress), and under lazy module loading (the CUDA default) it is
  * also when the library's device code and the 8 MiB array are loaded, the one call that
  * can allocate -- make it once at start-up, before any stream capture.  After
