@@ -631,8 +631,10 @@ template <class PS>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
   swr_pdl_entry();
   typedef Rec<PS> RL;
-  __shared__ float4 stage4[kSetupThreads * RL::R / 4];
-  float* stage = (float*)stage4;
+  // records staged with an odd stride, so the threads' scalar stores of one field fall in
+  // 32 different banks (a stride of R = 40 words put 32 threads in 4 banks)
+  constexpr int RS = RL::R + 1;
+  __shared__ float stage[kSetupThreads * RS];
   if (g.status[SWR_ST_FLAGS] & SWR_F_ANY_OVERFLOW) return;
   uint32_t np = g.status[SWR_ST_PRIMS];
   if (np > g.cap_prims) np = g.cap_prims;
@@ -670,7 +672,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
         for (int i = 0; i < RL::NP; ++i) pv[k][i] = i < g.vs_p ? vp[g.off_p + i] : 0.0f;
       }
     }
-    float* rec = stage + threadIdx.x * RL::R;
+    float* rec = stage + threadIdx.x * RS;
     uint32_t tiles = 0;
     // TriangleEquations: e0 = (v1, v2), e1 = (v2, v0), e2 = (v0, v1)
     const Edge e0 = make_edge(x[1], y[1], x[2], y[2]);
@@ -828,7 +830,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(SetupArgs g) {
   __syncthreads();
   const uint32_t cnt = min((uint32_t)kSetupThreads, np - p0);
   float4* dst = (float4*)(g.recs + (size_t)p0 * RL::R);
-  for (uint32_t i = threadIdx.x; i < cnt * (RL::R / 4); i += kSetupThreads) dst[i] = stage4[i];
+  for (uint32_t i = threadIdx.x; i < cnt * (RL::R / 4); i += kSetupThreads) {
+    const uint32_t t = i / (RL::R / 4);
+    const float* src = stage + t * RS + (i - t * (RL::R / 4)) * 4;
+    dst[i] = make_float4(src[0], src[1], src[2], src[3]);
+  }
   __syncthreads();
   }
 }
