@@ -46,8 +46,9 @@ uint32_t slice_cap(uint32_t ntiles) {
 // Descriptor upload from pinned host staging (device-accessible under unified addressing)
 // by a kernel rather than cudaMemcpyAsync: a copy-engine transfer would queue behind any
 // large host<->device copy the application runs on another stream, delaying the draw.
-// The same kernel zeroes the draw's small per-draw words (counters, single-draw bases), which
-// as separate memsets would each be one more operation (graph node) ahead of the draw.
+// The same kernel zeroes the draw's small per-draw words (counters, single-draw bases, the
+// heavy-tile list's length), which as separate memsets would each be one more operation (a
+// graph node, and a break in the kernels' programmatic dependent launches) ahead of the draw.
 struct StageCopy {
   void* dst[6];
   const void* src[6];
@@ -412,8 +413,8 @@ int raster_stage(swr_context* c, const PsOps* ps, int S, int off_a, int off_p, i
   const bool use_big = bm_bytes <= kBigSortSmem && c->big_cells.bytes >= (size_t)(ncells + 2) * 4;
   uint32_t* big = use_big ? c->big_cells.as<uint32_t>() : nullptr;
   // heavy tiles listed by k_sort_cells: rasterized in runs of chunks (depth-min shaders,
-  // tiles of more than one chunk), or else as quadrant CTAs (16-px tiles, shaders other
-  // than the overwrite ones; 8-px raster tiles split every tile)
+  // tiles of more than slice_chunks raster chunks), or else as quadrant CTAs (16-px tiles,
+  // shaders other than the overwrite ones; 8-px raster tiles split every tile)
   const int slice_chunks = c->dslice_chunks < 0 ? ps->slice_chunks : c->dslice_chunks;
   const bool dsl = ps->depth_min && slice_chunks > 0 && c->dslice_ok && c->quad_mode != 2;
   const bool quads = !dsl && c->tile == 16 && !ps->overwrite && c->quad_mode != 0;
