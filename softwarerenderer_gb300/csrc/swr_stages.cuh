@@ -1364,6 +1364,9 @@ __device__ __forceinline__ float build_z(const float* eq, bool blockmode, float 
 //      every covering fragment to the pixel's register-resident State: compacted fragments
 //      through apply(), others by rebuilding the interpolants in place (z first: a failing
 //      depth test needs nothing else) and drawPixel().
+// A heavy tile of a depth-min shader (RasterArgs.dslice) is run by up to SWR_DSLICES CTAs,
+// each over its own run of whole chunks from the draw's starting State; the last run to
+// finish merges the runs' States in bin order (swr_depth_merge) and stores.
 template <class PS, int TILE, int CH, bool SPAN>
 __global__ void __launch_bounds__(256, SWR_RASTER_MINB ? SWR_RASTER_MINB : SwrRasterOccupancy<PS>::value)
     k_raster(RasterArgs g) {
