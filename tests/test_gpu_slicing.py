@@ -49,3 +49,20 @@ def test_sliced_dense_mesh_matches_whole_tiles(gpu_lib, port, tile):
     whole, _ = gpu_render(sc, tile=tile, slicing=0)
     assert not diff(ref, got), [describe(ref, got, k) for k in diff(ref, got)]
     assert not diff(whole, got)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_sliced_batch_of_dense_meshes(gpu_lib, port, graph):
+    """A batch of three dense-mesh poses (the Lambert shader: heavy-tile runs on by default),
+    one target each: runs of tiles of different targets in one raster launch, captured and
+    replayed."""
+    from softwarerenderer_gb300.batch import BatchRenderer
+    scs = [scenes.sphere_scene(p, level=6, width=960, height=540) for p in (2, 9, 20)]
+    br = BatchRenderer(scs, aux=True, graph=graph)
+    refs = [oracle_render(port, sc)[0] for sc in scs]
+    for rep in range(2):  # with graph mode the second pass replays the graph
+        br.clear()
+        br.draw()
+        for sc, tg, ref in zip(scs, br.targets, refs):
+            got = tg.to_host()
+            assert not diff(ref, got), (rep, sc.name, [describe(ref, got, k) for k in diff(ref, got)])
